@@ -1,0 +1,208 @@
+// ed_api.cu -- the extern "C" boundary of libexactdiag_gb300.so.
+// Every entry point validates its arguments, returns an int status and never
+// lets a C++ exception or CUDA error escape; the text of the last failure is
+// kept per thread for ed_last_error_string().
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ed_internal.cuh"
+
+namespace ed {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int code, const char* what) {
+    g_last_error = what ? what : "";
+    return code;
+}
+
+int set_cuda_error(cudaError_t e, const char* what) {
+    g_last_error = std::string(what ? what : "") + ": " + cudaGetErrorString(e);
+    return ED_ERR_CUDA;
+}
+
+size_t hv_smem_bytes(const SectorView& S, size_t real_size);
+int hv_blocks_per_sm(const SectorView& S);
+
+static void host_comb(uint32_t c[kCombStride][kCombStride]) {
+    // c[k][n] = C(n, k) for n <= 32 (all values < 2^32)
+    uint64_t t[kCombStride][kCombStride];
+    std::memset(t, 0, sizeof(t));
+    for (int n = 0; n <= kMaxN; ++n) {
+        t[0][n] = 1;
+        for (int k = 1; k <= n; ++k) t[k][n] = t[k - 1][n - 1] + (k <= n - 1 ? t[k][n - 1] : 0);
+    }
+    for (int k = 0; k < kCombStride; ++k)
+        for (int n = 0; n < kCombStride; ++n) c[k][n] = (uint32_t)t[k][n];
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+struct ed_sector {
+    Sector s;
+};
+
+extern "C" {
+
+const char* ed_last_error_string(void) { return ed::g_last_error.c_str(); }
+
+int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out) {
+    if (!out) return set_error(ED_ERR_INVALID, "ed_sector_create: out is NULL");
+    *out = nullptr;
+    if (L < 2 || 2 * L > kMaxN) return set_error(ED_ERR_INVALID, "ed_sector_create: L must be in [2, 16]");
+    const int N = 2 * L;
+    if (Nh < 0 || Nh > N) return set_error(ED_ERR_INVALID, "ed_sector_create: Nh out of range");
+    if (Nd < 0 || Nd > N - Nh) return set_error(ED_ERR_INVALID, "ed_sector_create: Nd out of range");
+    if (ky != 0 && ky != 1) return set_error(ED_ERR_INVALID, "ed_sector_create: ky must be 0 or 1");
+    ed_sector* h = new (std::nothrow) ed_sector();
+    if (!h) return set_error(ED_ERR_NOMEM, "ed_sector_create: host allocation");
+    Sector& s = h->s;
+    uint32_t comb[kCombStride][kCombStride];
+    host_comb(comb);
+    SectorView& V = s.view;
+    V.L = L;
+    V.N = N;
+    V.Nh = Nh;
+    V.Nd = Nd;
+    V.Ns = N - Nh;
+    V.kx = ((kx % L) + L) % L;
+    V.ky = ky;
+    V.ne_even = ((N - Nh) % 2) == 0;
+    V.mask = (N == 32) ? 0xffffffffu : ((1u << N) - 1u);
+    s.kx_raw = kx;
+    s.real = ((2 * V.kx) % L) == 0;
+    s.n_spin = comb[Nd][N - Nh];
+    s.n_hole_masks = comb[Nh][N];
+    if (s.n_hole_masks > (int64_t(1) << 26)) {
+        delete h;
+        return set_error(ED_ERR_TOO_LARGE, "ed_sector_create: more than 2^26 hole masks");
+    }
+    cudaGetDevice(&s.device);
+    cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, s.device);
+    // colex spin-rank byte tables: T[c][k][byte]
+    std::vector<uint32_t> tab((size_t)4 * (Nd + 1) * 256, 0u);
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k <= Nd; ++k)
+            for (int byte = 0; byte < 256; ++byte) {
+                uint32_t r = 0;
+                int j = 0;
+                for (int b = 0; b < 8; ++b)
+                    if (byte & (1 << b)) {
+                        ++j;
+                        const int nn = 8 * c + b, kk = k + j;
+                        if (kk <= kMaxN) r += comb[kk][nn];
+                    }
+                tab[((size_t)c * (Nd + 1) + k) * 256 + byte] = r;
+            }
+    if (!s.d_comb.alloc(kCombStride * kCombStride) || !s.d_rank_tab.alloc((int64_t)tab.size())) {
+        delete h;
+        return set_error(ED_ERR_NOMEM, "ed_sector_create: device tables");
+    }
+    cudaError_t e1 = cudaMemcpy(s.d_comb.p, comb, sizeof(comb), cudaMemcpyHostToDevice);
+    cudaError_t e2 = cudaMemcpy(s.d_rank_tab.p, tab.data(), tab.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        delete h;
+        return set_cuda_error(e1 != cudaSuccess ? e1 : e2, "ed_sector_create: table upload");
+    }
+    V.comb = s.d_comb.p;
+    V.rank_tab = s.d_rank_tab.p;
+    *out = h;
+    return ED_OK;
+}
+
+int ed_sector_destroy(ed_sector* h) {
+    delete h;
+    return ED_OK;
+}
+
+int ed_basis_build(ed_sector* h, void* stream) {
+    if (!h) return set_error(ED_ERR_INVALID, "ed_basis_build: NULL sector");
+    Sector& s = h->s;
+    if (s.built) return ED_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc;
+    try {
+        rc = basis_build(s, st);
+    } catch (...) {
+        return set_error(ED_ERR_INTERNAL, "ed_basis_build: exception");
+    }
+    if (rc != ED_OK) return rc;
+    // persistent grid for the row kernels: SM count x resident CTAs per SM
+    int per_sm = hv_blocks_per_sm(s.view);
+    if (per_sm <= 0) per_sm = 1;
+    if (per_sm > 8) per_sm = 8;
+    s.hv_grid = s.num_sms * per_sm;
+    if (!s.d_partials.alloc((int64_t)s.hv_grid * kReduceSlots))
+        return set_error(ED_ERR_NOMEM, "ed_basis_build: reduction scratch");
+    return ED_OK;
+}
+
+int ed_basis_size(const ed_sector* h, int64_t* n) {
+    if (!h || !n) return set_error(ED_ERR_INVALID, "ed_basis_size: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_basis_size: basis not built");
+    *n = h->s.view.n;
+    return ED_OK;
+}
+
+int ed_sector_is_real(const ed_sector* h, int* is_real) {
+    if (!h || !is_real) return set_error(ED_ERR_INVALID, "ed_sector_is_real: NULL argument");
+    *is_real = h->s.real ? 1 : 0;
+    return ED_OK;
+}
+
+int ed_basis_export(const ed_sector* h, int64_t* sparse_dev, int32_t* orbit_dev, void* stream) {
+    if (!h || !sparse_dev || !orbit_dev) return set_error(ED_ERR_INVALID, "ed_basis_export: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_basis_export: basis not built");
+    return basis_export(const_cast<Sector&>(h->s), sparse_dev, orbit_dev, (cudaStream_t)stream);
+}
+
+static bool weights_ok(const double* w, HvWeights& out) {
+    if (!w) return false;
+    for (int t = 0; t < 4; ++t) {
+        if (!std::isfinite(w[t])) return false;
+        // matrix_setup.pyx:120-127 keeps terms with weight != 0 and
+        // sparse_matrices.py:89 skips |weight| < 1e-6
+        out.w[t] = (std::fabs(w[t]) < 1e-6) ? 0.0 : w[t];
+    }
+    return true;
+}
+
+int ed_hv(const ed_sector* h, const double weights[4], int dtype, const void* x_dev, void* y_dev, void* stream) {
+    if (!h || !x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_hv: basis not built");
+    HvWeights w;
+    if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_hv: weights");
+    if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv: x and y must not alias");
+    return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
+}
+
+int ed_lanczos_step(const ed_sector* h, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
+                    void* v_next_dev, double* scal_dev, void* stream) {
+    if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_step: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_step: basis not built");
+    HvWeights w;
+    if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_lanczos_step: weights");
+    if (v_dev == v_next_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_step: v and v_next must not alias");
+    return lanczos_step_launch(h->s, w, dtype, v_dev, v_prev_dev, v_next_dev, scal_dev, h->s.d_partials.p,
+                               (cudaStream_t)stream);
+}
+
+int ed_normalize(const ed_sector* h, int dtype, void* x_dev, double* norm_dev, void* stream) {
+    if (!h || !x_dev || !norm_dev) return set_error(ED_ERR_INVALID, "ed_normalize: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_normalize: basis not built");
+    return normalize_launch(h->s, dtype, x_dev, norm_dev, h->s.d_partials.p, (cudaStream_t)stream);
+}
+
+int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const double* omega_dev, int W, double e0,
+                          double eta, double norm2, double* out_dev, void* stream) {
+    if (!a_dev || !b_dev || !omega_dev || !out_dev) return set_error(ED_ERR_INVALID, "ed_continued_fraction: NULL");
+    return cf_launch(a_dev, b_dev, m, omega_dev, W, e0, eta, norm2, out_dev, (cudaStream_t)stream);
+}
+
+}  // extern "C"

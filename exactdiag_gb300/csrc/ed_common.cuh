@@ -1,0 +1,221 @@
+// ed_common.cuh -- bit-level state model of the spin-1/2 t-J two-leg ladder
+// shared by the basis, H.v, Lanczos and excitation kernels.
+//
+// A configuration of N = 2L sites (site i = 2x + y, rung x, leg y) is two
+// N-bit masks: h (holes) and d (down spins); every other site is an up spin.
+// The packed key (h << 32) | d orders configurations exactly like the
+// reference's sparse index (hole rank * C(Ns,Nd) + spin rank,
+// tJ_spin_half_ladder/symmetry_ladder.h:346-361): colex rank is monotone in the
+// mask value, holes are compared first, and for equal hole masks the raw down
+// mask orders like its compressed form.  State_Hierarchy::check_lower_state
+// (general/group/commutation_counter.h:45-69) therefore becomes a 64-bit compare.
+//
+// Symmetry group (2L elements, product index p = 1..N-1 in the reference's
+// order, general/cpp_classes.h:14-105): translation by s = p/2 rungs is a
+// rotation of both masks by 2s bits; odd p first swaps the two legs (even and
+// odd bits).  Amplitudes are powers of u = exp(-i*pi/L); an amplitude is held
+// as its exponent e mod 2L, which makes the reference's |amp - 1| > 1e-8 tests
+// (symmetry_ladder.h:196-224) exact integer tests.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ed {
+
+constexpr int kMaxN = 32;
+constexpr int kCombStride = 33;
+
+enum : uint32_t { kBlockFree = 1u };
+
+// One eligible (canonical) hole mask: a contiguous range of dense rows.
+struct BlockInfo {
+    uint32_t hmask;     // canonical hole mask of the block
+    uint32_t flags;     // kBlockFree: trivial stabiliser -> every spin rank is a representative
+    int64_t start;      // first dense row of the block
+    int64_t count;      // rows in the block
+    int64_t word_off;   // first word of the block's candidate bitmap (non-free blocks), else -1
+};
+
+// One hole mask (any, indexed by its colex rank): how it maps to its canonical block.
+struct HoleEntry {
+    int32_t block;      // block of the canonical mask, -1 if the canonical mask has no block
+    uint8_t p_star;     // product index whose image carries the canonical mask (free masks)
+    uint8_t e_star;     // phase exponent of that image (free masks)
+    uint8_t free_;      // 1 if the canonical mask has a trivial stabiliser
+    uint8_t pad_;
+};
+
+// Read-only view of a built sector, passed to kernels by value.
+struct SectorView {
+    int L, N, Nh, Nd, Ns;
+    int kx;                 // leg momentum mod L
+    int ky;                 // rung parity
+    int ne_even;            // number of electrons even
+    uint32_t mask;          // low N bits
+    int64_t n;              // number of representatives
+    int64_t n_hole_masks;   // C(N, Nh) (size of `holes`, 0 when no table)
+    int n_blocks;
+    const BlockInfo* blocks;
+    const HoleEntry* holes;        // may be null: generic mode (block found by binary search)
+    const uint64_t* keys;          // [n] packed representative keys, ascending
+    const uint8_t* orbit;          // [n] orbit size (num_sparse_states_in_dense)
+    const uint64_t* bitmap;        // candidate bitmaps of non-free blocks
+    const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word
+    const uint32_t* rank_tab;      // [4][Nd+1][256] byte tables of the colex spin rank
+    const uint32_t* comb;          // [33][33] comb[k*33+n] = C(n,k)
+};
+
+// ---------------------------------------------------------------- bit helpers
+
+__host__ __device__ __forceinline__ uint32_t rotl_n(uint32_t x, int r, int N, uint32_t mask) {
+    uint64_t xx = x;
+    return (uint32_t)(((xx << r) | (xx >> (N - r))) & mask);
+}
+
+__host__ __device__ __forceinline__ uint32_t mirror_legs(uint32_t x) {
+    return ((x & 0x55555555u) << 1) | ((x >> 1) & 0x55555555u);
+}
+
+// Image of (h, d) under product index p (0 = identity).
+__host__ __device__ __forceinline__ void apply_p(int p, uint32_t& h, uint32_t& d, int N, uint32_t mask) {
+    if (p & 1) {
+        h = mirror_legs(h);
+        d = mirror_legs(d);
+    }
+    const int r = 2 * (p >> 1);
+    h = rotl_n(h, r, N, mask);
+    d = rotl_n(d, r, N, mask);
+}
+
+__host__ __device__ __forceinline__ int ctz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __ffs(x) - 1;
+#else
+    return __builtin_ctz(x);
+#endif
+}
+__host__ __device__ __forceinline__ int popc32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+__host__ __device__ __forceinline__ int hibit32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return 31 - __clz(x);
+#else
+    return 31 - __builtin_clz(x);
+#endif
+}
+
+// Remove the bits at hole positions (parallel bit extract over ~h).
+__host__ __device__ __forceinline__ uint32_t compress_spins(uint32_t d, uint32_t h) {
+    while (h) {
+        const int p = hibit32(h);
+        h &= ~(1u << p);
+        const uint32_t low = (1u << p) - 1u;
+        d = (d & low) | ((d >> 1) & ~low);
+    }
+    return d;
+}
+
+// Colex rank of a compressed down mask from byte tables:
+// T[(c*(Nd+1) + k)*256 + byte] = sum over the set bits of `byte` (j-th from
+// the bottom) of C(8c + bitpos, k + j).
+__host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const uint32_t* T, int Nd) {
+    uint32_t r = 0;
+    int k = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const uint32_t byte = (dc >> (8 * c)) & 255u;
+        r += T[(c * (Nd + 1) + k) * 256 + byte];
+        k += popc32(byte);
+        if (k > Nd) k = Nd;
+    }
+    return r;
+}
+
+// Colex rank of a hole mask (general/symmetry_ladder.h:346-361, hole part).
+__host__ __device__ __forceinline__ uint32_t hole_rank(uint32_t h, const uint32_t* comb) {
+    uint32_t r = 0;
+    int j = 0;
+    while (h) {
+        const int p = ctz32(h);
+        h &= h - 1u;
+        ++j;
+        r += comb[j * kCombStride + p];
+    }
+    return r;
+}
+
+// --------------------------------------------------------------- orbit walk
+
+struct OrbitResult {
+    int found;      // orbit size as the reference counts it, 0 = not lowest / incompatible
+    uint64_t low;   // lowest image (first strictly-lowest in the reference's list order)
+    int e;          // phase exponent of the lowest image, mod 2L
+};
+
+// Restatement of Symmetries_Single_Spin_Half_2leg_Ladder::get_symmetry_states_from_state
+// (tJ_spin_half_ladder/symmetry_ladder.h:113-235) on packed keys, followed by
+// the lowest-image pick of get_lowest_sparse_amplitude_from_state
+// (general/symmetry.h:97-126).  Same iteration order, same early exits, same
+// orbit-closure rule (only while s < L/2 + 1).
+__host__ __device__ __forceinline__ OrbitResult orbit_walk(int L, int kx, int ky, int ne_even, uint32_t mask, uint32_t h,
+                                                           uint32_t d, bool check_lowest) {
+    const int N = 2 * L, twoL = 2 * L;
+    const uint64_t key = ((uint64_t)h << 32) | d;
+    const uint32_t any_hole = (h | (h >> 1)) & 0x55555555u & mask;
+    const uint32_t single = (h ^ (h >> 1)) & 0x55555555u & mask;
+    const int P = L - popc32(any_hole);
+    const int e_mirror = (L * ky + L * (P & 1)) % twoL;
+    const uint32_t hm = mirror_legs(h), dm = mirror_legs(d);
+    int eT = 0, found = 1, e1 = 0, elow = 0;
+    bool msym = false;
+    uint64_t img1 = 0, low = key;
+    for (int p = 1; p < N; ++p) {
+        const int s = p >> 1;
+        uint64_t img;
+        int e;
+        if (p & 1) {
+            if (msym) continue;
+            img = ((uint64_t)rotl_n(hm, 2 * s, N, mask) << 32) | rotl_n(dm, 2 * s, N, mask);
+            e = eT + e_mirror;
+            if (e >= twoL) e -= twoL;
+        } else {
+            img = ((uint64_t)rotl_n(h, 2 * s, N, mask) << 32) | rotl_n(d, 2 * s, N, mask);
+            eT += 2 * kx;
+            if (ne_even && ((single >> (2 * (L - s))) & 1u)) eT += L;
+            eT %= twoL;
+            e = eT;
+        }
+        if (check_lowest && img < key) return {0, 0, 0};
+        if (s < L / 2 + 1) {
+            if (img == key) {
+                if (e != 0) return {0, 0, 0};
+                if (p == 1) {
+                    msym = true;
+                    continue;
+                }
+                break;
+            }
+            if (found != 1 && img == img1) {
+                if (e != e1) return {0, 0, 0};
+                break;
+            }
+        }
+        if (found == 1) {
+            img1 = img;
+            e1 = e;
+        }
+        ++found;
+        if (img < low) {
+            low = img;
+            elow = e;
+        }
+    }
+    return {found, low, elow};
+}
+
+}  // namespace ed

@@ -1,0 +1,107 @@
+// ed_internal.cuh -- host-side sector object, device buffers and error plumbing
+// shared by the translation units of libexactdiag_gb300.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/exactdiag_gb300.h"
+#include "ed_common.cuh"
+
+namespace ed {
+
+// Thread-local error text behind ed_last_error_string().
+int set_error(int code, const char* what);
+int set_cuda_error(cudaError_t e, const char* what);
+
+#define ED_CHECK_LAUNCH(name)                                           \
+    do {                                                                \
+        cudaError_t e_ = cudaGetLastError();                            \
+        if (e_ != cudaSuccess) return ::ed::set_cuda_error(e_, name);   \
+    } while (0)
+
+// Owning device buffer; frees on destruction.  Allocation failure leaves p null.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    int64_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(int64_t count) { alloc(count); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    bool alloc(int64_t count) {
+        reset();
+        if (count <= 0) count = 1;
+        // 64-bit size check before cudaMalloc
+        if ((uint64_t)count > UINT64_MAX / sizeof(T)) return false;
+        if (cudaMalloc((void**)&p, (size_t)count * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return false;
+        }
+        n = count;
+        return true;
+    }
+    bool ok() const { return p != nullptr; }
+};
+
+inline int grid_for(int64_t work, int threads, int sms, int per_sm = 8) {
+    int64_t g = (work + threads - 1) / threads;
+    const int64_t cap = (int64_t)sms * per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+constexpr int kHvThreads = 256;
+constexpr int kReduceSlots = 4;  // FP64 partial sums per CTA in the fused Lanczos step
+
+struct Sector {
+    SectorView view{};
+    int64_t n_hole_masks = 0;
+    uint64_t n_spin = 0;
+    int kx_raw = 0;
+    bool real = false;
+    bool built = false;
+    int device = 0;
+    int num_sms = 152;
+    int hv_grid = 0;             // persistent grid of the H.v kernels
+    DevBuf<uint32_t> d_comb;     // [33][33]
+    DevBuf<uint32_t> d_rank_tab; // [4][Nd+1][256]
+    DevBuf<BlockInfo> d_blocks;
+    DevBuf<HoleEntry> d_holes;
+    DevBuf<uint64_t> d_bitmap;
+    DevBuf<int64_t> d_prefix;
+    DevBuf<uint64_t> d_keys;
+    DevBuf<uint8_t> d_orbit;
+    DevBuf<double> d_partials;   // [hv_grid][kReduceSlots] scratch of the fused Lanczos step
+};
+
+// ed_basis.cu
+int basis_build(Sector& s, cudaStream_t st);
+int basis_export(Sector& s, int64_t* sparse_dev, int32_t* orbit_dev, cudaStream_t st);
+void pack_flags(const uint8_t* f, int64_t n, uint64_t* words, cudaStream_t st, int sms);
+void expand_flag_scan(const uint8_t* f, int64_t n, const uint64_t* words, const int64_t* wprefix, int64_t* out,
+                      cudaStream_t st, int sms);
+int scan_popcounts(const uint64_t* words, int64_t m, int64_t* prefix, int64_t* total_host, cudaStream_t st);
+
+// ed_hv.cu
+struct HvWeights {
+    double w[4];  // tl, tr, jl, jr; 0 disables a term
+};
+int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st);
+int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev,
+                        void* vnext, double* scal, double* partials, cudaStream_t st);
+int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
+int cf_launch(const double* a, const double* b, int m, const double* omega, int W, double e0, double eta,
+              double norm2, double* out, cudaStream_t st);
+
+}  // namespace ed

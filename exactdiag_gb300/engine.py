@@ -1,0 +1,152 @@
+"""Device sectors: the Python face of the C ABI (include/exactdiag_gb300.h).
+
+PyTorch provides device memory and the current CUDA stream; every operation on
+the path is a call into libexactdiag_gb300.so.  Vectors are torch tensors on the
+sector's device, indexed by dense basis index (the reference's own order).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from exactdiag_gb300 import _native as nat
+
+TERMS = ("tl", "tr", "jl", "jr")
+
+# (dtype code, torch dtype) per precision and sector kind
+_DTYPES = {
+    ("fp64", True): (nat.ED_F64, torch.float64),
+    ("fp64", False): (nat.ED_C128, torch.complex128),
+    ("fp32", True): (nat.ED_F32, torch.float32),
+    ("fp32", False): (nat.ED_C64, torch.complex64),
+}
+_CODE_OF_TORCH = {torch.float64: nat.ED_F64, torch.complex128: nat.ED_C128, torch.float32: nat.ED_F32,
+                  torch.complex64: nat.ED_C64}
+
+
+def _stream_ptr() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def weights_tuple(weights) -> tuple[float, float, float, float]:
+    """(tl, tr, jl, jr) from a mapping, an object with those attributes, or a 4-sequence."""
+    if isinstance(weights, dict):
+        return tuple(float(weights.get(t, 0.0)) for t in TERMS)
+    if hasattr(weights, "tl"):
+        return tuple(float(getattr(weights, t)) for t in TERMS)
+    w = tuple(float(v) for v in weights)
+    if len(w) != 4:
+        raise ValueError("weights must have 4 entries (tl, tr, jl, jr)")
+    return w
+
+
+@dataclass(frozen=True)
+class SectorKey:
+    num_rungs: int
+    num_holes: int
+    num_down_spins: int
+    kx: int
+    ky: int
+
+
+class DeviceSector:
+    """A symmetry sector whose basis lives on the GPU (ed_sector_create + ed_basis_build)."""
+
+    def __init__(self, num_rungs: int, num_holes: int, num_down_spins: int, kx: int, ky: int):
+        if not torch.cuda.is_available():
+            raise RuntimeError("exactdiag_gb300 needs a CUDA device; there is no CPU path")
+        self._lib = nat.load()
+        self.key = SectorKey(int(num_rungs), int(num_holes), int(num_down_spins), int(kx), int(ky))
+        h = ctypes.c_void_p()
+        nat.check("ed_sector_create",
+                  self._lib.ed_sector_create(self.key.num_rungs, self.key.num_holes, self.key.num_down_spins,
+                                             self.key.kx, self.key.ky, ctypes.byref(h)))
+        self._h = h
+        nat.check("ed_basis_build", self._lib.ed_basis_build(h, _stream_ptr()))
+        n = ctypes.c_int64()
+        nat.check("ed_basis_size", self._lib.ed_basis_size(h, ctypes.byref(n)))
+        self.n = int(n.value)
+        r = ctypes.c_int()
+        nat.check("ed_sector_is_real", self._lib.ed_sector_is_real(h, ctypes.byref(r)))
+        self.is_real = bool(r.value)
+        self.device = torch.device("cuda", torch.cuda.current_device())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ed_sector_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def dtype(self, precision: str = "fp64") -> torch.dtype:
+        return _DTYPES[(precision, self.is_real)][1]
+
+    def export_basis(self) -> tuple[np.ndarray, np.ndarray]:
+        """(dense_to_sparse int64, num_sparse_in_dense int32) in the reference's format."""
+        sp = torch.empty(max(self.n, 1), dtype=torch.int64, device=self.device)
+        orb = torch.empty(max(self.n, 1), dtype=torch.int32, device=self.device)
+        nat.check("ed_basis_export", self._lib.ed_basis_export(self._h, _ptr(sp), _ptr(orb), _stream_ptr()))
+        return sp[: self.n].cpu().numpy(), orb[: self.n].cpu().numpy()
+
+    def _code(self, t: torch.Tensor) -> int:
+        code = _CODE_OF_TORCH.get(t.dtype)
+        if code is None:
+            raise TypeError(f"unsupported vector dtype {t.dtype}")
+        if not t.is_cuda or not t.is_contiguous() or t.numel() != self.n:
+            raise ValueError("vectors must be contiguous CUDA tensors of length n")
+        return code
+
+    def hv(self, x: torch.Tensor, weights, out: torch.Tensor | None = None) -> torch.Tensor:
+        """y = H x (ed_hv)."""
+        code = self._code(x)
+        y = torch.empty_like(x) if out is None else out
+        self._code(y)
+        w = nat.weights_array(weights_tuple(weights))
+        nat.check("ed_hv", self._lib.ed_hv(self._h, w, code, _ptr(x), _ptr(y), _stream_ptr()))
+        return y
+
+    def lanczos_step(self, weights, v: torch.Tensor, v_prev: torch.Tensor | None, v_next: torch.Tensor,
+                     scal: torch.Tensor) -> None:
+        """One fused step (ed_lanczos_step); scal is a float64 CUDA tensor of length >= 4."""
+        code = self._code(v)
+        self._code(v_next)
+        if v_prev is not None:
+            self._code(v_prev)
+        if scal.dtype != torch.float64 or not scal.is_cuda or scal.numel() < 4:
+            raise ValueError("scal must be a float64 CUDA tensor with 4 entries")
+        w = nat.weights_array(weights_tuple(weights))
+        nat.check("ed_lanczos_step",
+                  self._lib.ed_lanczos_step(self._h, w, code, _ptr(v), _ptr(v_prev), _ptr(v_next),
+                                            _ptr(scal), _stream_ptr()))
+
+    def normalize(self, x: torch.Tensor, norm_out: torch.Tensor) -> None:
+        code = self._code(x)
+        nat.check("ed_normalize", self._lib.ed_normalize(self._h, code, _ptr(x), _ptr(norm_out), _stream_ptr()))
+
+
+def continued_fraction(a: torch.Tensor, b: torch.Tensor, omegas: torch.Tensor, e0: float, eta: float,
+                       norm2: float) -> torch.Tensor:
+    """S(omega) on the device (ed_continued_fraction); a, b, omegas float64 CUDA tensors."""
+    lib = nat.load()
+    out = torch.empty_like(omegas)
+    m = int(a.numel())
+    nat.check("ed_continued_fraction",
+              lib.ed_continued_fraction(_ptr(a), _ptr(b), m, _ptr(omegas), int(omegas.numel()), float(e0),
+                                        float(eta), float(norm2), _ptr(out), _stream_ptr()))
+    return out

@@ -1,0 +1,105 @@
+/*
+ * exactdiag_gb300.h -- C ABI of the GB300 t-J ladder engine (libexactdiag_gb300.so).
+ *
+ * The engine replaces four native pieces of exactdiag's hot path; each entry
+ * point below names the reference interface it stands in for (paths inside
+ * the reference project).  Conventions:
+ *   - every function returns an int status: ED_OK (0) or a negative ED_ERR_*;
+ *     ed_last_error_string() gives a thread-local description;
+ *   - no exception, C++ type or torch type crosses this boundary;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream);
+ *   - pointers named *_dev are device memory owned by the caller; *_host are host memory;
+ *   - vectors are indexed by the dense basis index, i.e. in the reference's
+ *     own order (ascending sparse index, general/basis_indexing.h:188-242).
+ */
+#ifndef EXACTDIAG_GB300_H
+#define EXACTDIAG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ED_OK 0
+#define ED_ERR_INVALID (-1)   /* bad argument */
+#define ED_ERR_NOMEM (-2)     /* device allocation failed */
+#define ED_ERR_CUDA (-3)      /* CUDA runtime error */
+#define ED_ERR_NOT_BUILT (-4) /* ed_basis_build has not run */
+#define ED_ERR_TOO_LARGE (-5) /* sector exceeds a supported table size */
+#define ED_ERR_INTERNAL (-6)  /* an internal consistency check failed */
+#define ED_ERR_TIMEOUT (-7)   /* a bounded device-side wait gave up */
+
+/* Arithmetic types of the vectors passed to the operator entry points. */
+#define ED_F64 0 /* double, real sectors (k_x in {0, L/2}) */
+#define ED_C128 1 /* interleaved complex double */
+#define ED_F32 2 /* float, real sectors */
+#define ED_C64 3 /* interleaved complex float */
+
+typedef struct ed_sector ed_sector;
+
+/* Sector of the periodic two-leg ladder: L rungs (1..16), Nh holes, Nd down
+ * spins, leg momentum kx (any integer, taken mod L) and rung parity ky (0/1).
+ * Stands in for Hamiltonian_Config.get_translators()
+ * (tJ_spin_half_ladder/matrix_setup.pyx:377-406), which builds
+ * State_Index_Amplitude_Translator (symmetry_ladder.h:271-406) and
+ * Symmetries_Single_Spin_Half_2leg_Ladder (symmetry_ladder.h:55-269). */
+int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out);
+int ed_sector_destroy(ed_sector* s);
+
+/* Enumerates the representatives on the device.  Replaces get_basis_map /
+ * calc_basis_map (general/basis_indexing.h:188-261). Synchronises `stream`. */
+int ed_basis_build(ed_sector* s, void* stream);
+
+/* Number of representatives (Basis_Index_Map::get_num_states, basis_indexing.h:180-182). */
+int ed_basis_size(const ed_sector* s, int64_t* n);
+
+/* 1 if the sector's matrix elements are real (k_x*2 = 0 mod L), else 0. */
+int ed_sector_is_real(const ed_sector* s, int* is_real);
+
+/* Writes the basis in the reference's format: dense_to_sparse (int64 sparse
+ * index) and num_sparse_states_in_dense (int32 orbit size), device arrays of
+ * length n (Basis_Index_Map fields, basis_indexing.h:31-46, saved layout :128-146). */
+int ed_basis_export(const ed_sector* s, int64_t* sparse_dev, int32_t* orbit_dev, void* stream);
+
+/* y = H x with H = sum_t weights[t] * term_t, t in (tl, tr, jl, jr), applied
+ * matrix-free and pull-style (no atomics, deterministic).  Replaces
+ * Added_Sparse_Matrices.dot (general/sparse_matrices.py:233-237) ->
+ * sparse_matrix_dot (general/cython_sparse_dot.pyx:40-80) over the terms built
+ * by setup_hamiltonian (tJ_spin_half_ladder/matrix_setup.pyx:41-129).
+ * dtype is ED_F64/ED_C128/ED_F32/ED_C64; real dtypes require a real sector. */
+int ed_hv(const ed_sector* s, const double weights[4], int dtype, const void* x_dev, void* y_dev, void* stream);
+
+/* One Lanczos step of the spectrum recursion
+ * (general/cython_lanczos_diagonalization.pyx:68-77 _lanczos_vec_iteration):
+ *   w = H v_k,  a_k = Re<v_k, w>,  v' = w - a_k v_k - b_k v_{k-1},
+ *   b_{k+1} = |v'|,  v_{k+1} = v' / b_{k+1}.
+ * scal_dev is a device double array: scal_dev[0] = b_k (read), on return
+ * scal_dev[1] = a_k and scal_dev[2] = b_{k+1} (written on the device; nothing is
+ * copied to the host, so the call can be captured in a CUDA graph).  v_prev may
+ * be NULL (b_k ignored).  v_next receives v_{k+1}; it may alias v_prev.  The
+ * products are accumulated in FP64 whatever dtype is.  When b_{k+1} < 1e-8
+ * (the reference's breakdown test, :63-64) v_next is left as v' unnormalised
+ * and scal_dev[3] is set to 1. */
+int ed_lanczos_step(const ed_sector* s, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
+                    void* v_next_dev, double* scal_dev, void* stream);
+
+/* Scales x in place to unit norm (FP64 accumulation); norm written to norm_dev[0]. */
+int ed_normalize(const ed_sector* s, int dtype, void* x_dev, double* norm_dev, void* stream);
+
+/* Continued fraction S(w) = -(1/pi) * norm2 * Im[1 / (z - a_0 - b_1^2/(z - a_1 - ...))],
+ * z = omega + e0 + i*eta, evaluated bottom-up for every omega
+ * (general/cython_lanczos_diagonalization.pyx:42-48, :36-39 and
+ * general/lanczos_diagonalization.py:158-175).  a_dev[m], b_dev[m] (b[0]
+ * unused), omega_dev[W], out_dev[W]: device doubles. */
+int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const double* omega_dev, int W, double e0,
+                          double eta, double norm2, double* out_dev, void* stream);
+
+/* Thread-local description of the last error. */
+const char* ed_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXACTDIAG_GB300_H */

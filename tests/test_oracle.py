@@ -1,0 +1,125 @@
+"""CPU: pin the oracle against the reference's fixtures, its compiled code and the golden vectors."""
+
+import numpy as np
+import pytest
+import scipy.special
+
+from conftest import fixture_sector, seeded_vector
+
+EIGENVALUE_TOLERANCE = 1e-8  # tests/tJ_spin_half_ladder/test_eigvals.py:6
+
+
+def test_basis_sizes_match_reference_fixtures(oracle, reference_fixtures):
+    assert len(reference_fixtures) == 68
+    for d in reference_fixtures:
+        sp, orb = oracle.basis(oracle.Sector(*fixture_sector(d)))
+        assert len(sp) == d["basis_size"], d["file"]
+
+
+def test_eigenvalues_match_reference_fixtures(oracle, reference_fixtures):
+    checked = 0
+    for d in reference_fixtures:
+        if d.get("eigvals") is None:
+            continue
+        sec = oracle.Sector(*fixture_sector(d))
+        bas = oracle.basis(sec)
+        h = oracle.hamiltonian(sec, d["weights"], bas)
+        ev = oracle.lowest_eigvals(h, len(d["eigvals"]))
+        assert np.all(np.abs(ev - np.array(d["eigvals"])) < EIGENVALUE_TOLERANCE), d["file"]
+        checked += 1
+    assert checked == 51
+
+
+def test_sum_over_k_matches_combinatorics(oracle):
+    # tests/tJ_spin_half_ladder/test_basis_size.py:61-113 invariants
+    for L, Nh in [(4, 2), (5, 1), (6, 0), (6, 3)]:
+        N = 2 * L
+        for Nd in range(N - Nh + 1):
+            total = 0
+            for kx in range(L // 2 + 1):
+                mult = 1 + (kx != 0 and (kx != L // 2 or L % 2))
+                for ky in (0, 1):
+                    total += mult * len(oracle.basis(oracle.Sector(L, Nh, Nd, kx, ky))[0])
+            assert total == scipy.special.comb(N, Nh, exact=True) * scipy.special.comb(N - Nh, Nd, exact=True)
+
+
+def test_negative_and_periodic_k(oracle):
+    for kx in range(1, 4):
+        for ky in (0, 1):
+            n = len(oracle.basis(oracle.Sector(6, 0, 6, kx, ky))[0])
+            assert len(oracle.basis(oracle.Sector(6, 0, 6, -kx, ky))[0]) == n
+            for mult in (-2, 1, 3):
+                assert len(oracle.basis(oracle.Sector(6, 0, 6, kx + 6 * mult, ky))[0]) == n
+
+
+def test_term_matrices_are_hermitian(oracle):
+    for key in [(5, 2, 4, 1, 1), (6, 1, 5, 2, 0), (4, 0, 4, 1, 1)]:
+        sec = oracle.Sector(*key)
+        bas = oracle.basis(sec)
+        n = len(bas[0])
+        import scipy.sparse as sps
+
+        for t in oracle.TERMS:
+            cp, r, v = oracle.term_columns(sec, t, bas, triangle=False)
+            m = sps.csc_matrix((v, r, cp), shape=(n, n))
+            if m.nnz:
+                assert abs(m - m.conj().T).max() < 1e-13
+
+
+def test_oracle_matches_golden(oracle, golden_sectors):
+    secs = golden_sectors["sectors"]
+    w = dict(zip(oracle.TERMS, golden_sectors["weights"]))
+    for key in secs:
+        key = tuple(int(v) for v in key)
+        tag = "s%d_%d_%d_%d_%d" % key
+        sec = oracle.Sector(*key)
+        sp, orb = oracle.basis(sec)
+        assert np.array_equal(sp, golden_sectors[f"{tag}_sparse"])
+        assert np.array_equal(orb, golden_sectors[f"{tag}_orbit"].astype(np.int32))
+        h = oracle.hamiltonian(sec, w, (sp, orb))
+        real = (2 * (key[3] % key[0])) % key[0] == 0
+        seed = int(golden_sectors[f"{tag}_seed"][0])
+        y = h @ seeded_vector(len(sp), seed, not real)
+        assert np.max(np.abs(y - golden_sectors[f"{tag}_y"])) < 1e-12
+
+
+def test_oracle_excitations_match_golden(oracle, golden_excitations):
+    names = {0: "Szq", 1: "spectral_function_minus"}
+    for idx, case in enumerate(golden_excitations["cases"]):
+        L, Nh, Nd, kx, ky, op, qx, qy = (int(v) for v in case)
+        sec = oracle.Sector(L, Nh, Nd, kx, ky)
+        bas = oracle.basis(sec)
+        fsec = oracle.target_sector(sec, names[op], qx, qy)
+        assert list(fsec.args()) == list(golden_excitations[f"e{idx}_target"])
+        fbas = oracle.basis(fsec)
+        m = oracle.excitation_matrix(sec, bas, names[op], qx, qy, fsec, fbas)
+        y = m @ seeded_vector(len(bas[0]), int(golden_excitations[f"e{idx}_seed"][0]), True)
+        assert np.max(np.abs(y - golden_excitations[f"e{idx}_y"])) < 1e-12
+
+
+def test_oracle_bit_exact_against_reference_code(oracle):
+    if not oracle.REF_SRC.is_dir():
+        pytest.skip("reference tree absent: oracle/_ref cannot be built here")
+    oracle.build(ref=True)
+    if oracle.ref_lib() is None:
+        pytest.skip("oracle/_ref not built")
+    for key in [(4, 2, 3, 1, 0), (5, 2, 4, 2, 1), (6, 0, 6, 1, 1), (6, 3, 4, 0, 0), (7, 1, 6, 3, 1)]:
+        sec = oracle.Sector(*key)
+        a = oracle.basis(sec)
+        b = oracle.basis(sec, impl="ref")
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        for t in oracle.TERMS:
+            c1 = oracle.term_columns(sec, t, a)
+            c2 = oracle.term_columns(sec, t, a, impl="ref")
+            assert np.array_equal(c1[0], c2[0]) and np.array_equal(c1[1], c2[1])
+            assert np.max(np.abs(c1[2] - c2[2]), initial=0) < 1e-14
+
+
+def test_continued_fraction_restatement(oracle):
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-2, 2, 40)
+    b = np.concatenate([[0.0], rng.uniform(0.1, 1.0, 39)])
+    zs = np.linspace(-3, 3, 17) + 0.1j
+    vec = oracle.continued_fraction(a, b, zs, 2.5)
+    for k, z in enumerate(zs):
+        assert abs(vec[k] - (-1 / np.pi * 2.5 * oracle.spectral_value_at_z(a, b, z))) < 1e-12

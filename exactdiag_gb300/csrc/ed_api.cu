@@ -193,6 +193,32 @@ int ed_lanczos_step(const ed_sector* h, const double weights[4], int dtype, cons
                                (cudaStream_t)stream);
 }
 
+int ed_lanczos_hv(const ed_sector* h, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
+                  void* v_next_dev, double* scal_dev, void* stream) {
+    if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_hv: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_hv: basis not built");
+    HvWeights w;
+    if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_lanczos_hv: weights");
+    if (v_dev == v_next_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_hv: v and v_next must not alias");
+    return lanczos_hv_launch(h->s, w, dtype, v_dev, v_prev_dev, v_next_dev, scal_dev, h->s.d_partials.p,
+                             (cudaStream_t)stream);
+}
+
+int ed_lanczos_update(const ed_sector* h, int dtype, const void* v_dev, void* v_next_dev, const double* scal_dev,
+                      void* stream) {
+    if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_update: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_update: basis not built");
+    return lanczos_update_launch(h->s, dtype, v_dev, v_next_dev, scal_dev, (cudaStream_t)stream);
+}
+
+int ed_accumulate(const ed_sector* h, int dtype, const void* x_dev, double coef_re, double coef_im, void* acc_dev,
+                  void* stream) {
+    if (!h || !x_dev || !acc_dev) return set_error(ED_ERR_INVALID, "ed_accumulate: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_accumulate: basis not built");
+    if (!std::isfinite(coef_re) || !std::isfinite(coef_im)) return set_error(ED_ERR_INVALID, "ed_accumulate: coef");
+    return accumulate_launch(h->s, dtype, x_dev, coef_re, coef_im, acc_dev, (cudaStream_t)stream);
+}
+
 int ed_normalize(const ed_sector* h, int dtype, void* x_dev, double* norm_dev, void* stream) {
     if (!h || !x_dev || !norm_dev) return set_error(ED_ERR_INVALID, "ed_normalize: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_normalize: basis not built");

@@ -480,29 +480,83 @@ int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, voi
 }
 
 template <typename R, bool CPLX>
-static int step_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext, double* scal,
-                      double* partials, cudaStream_t st) {
+static int step_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
+                         double* scal, double* partials, cudaStream_t st) {
     const size_t smem = hv_smem_bytes(s.view, sizeof(R));
     cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     lanczos_hv_kernel<R, CPLX><<<s.hv_grid, kHvThreads, smem, st>>>(s.view, w, v, vprev, vnext, scal, partials);
     ED_CHECK_LAUNCH("lanczos_hv_kernel");
     lanczos_scalars_kernel<<<1, 256, 0, st>>>(partials, s.hv_grid, scal);
     ED_CHECK_LAUNCH("lanczos_scalars_kernel");
+    return ED_OK;
+}
+
+template <typename R, bool CPLX>
+static int step_update_typed(const Sector& s, const void* v, void* vnext, const double* scal, cudaStream_t st) {
     lanczos_update_kernel<R, CPLX><<<grid_for(s.view.n, 256, s.num_sms, 16), 256, 0, st>>>(s.view.n, v, vnext, scal);
     ED_CHECK_LAUNCH("lanczos_update_kernel");
     return ED_OK;
 }
 
-int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
-                        double* scal, double* partials, cudaStream_t st) {
+int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
+                      double* scal, double* partials, cudaStream_t st) {
     if (!dtype_ok(s, dtype)) return set_error(ED_ERR_INVALID, "ed_lanczos_step: dtype does not match the sector");
     if (s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_lanczos_step: empty sector");
     switch (dtype) {
-    case ED_F64: return step_typed<double, false>(s, w, v, vprev, vnext, scal, partials, st);
-    case ED_C128: return step_typed<double, true>(s, w, v, vprev, vnext, scal, partials, st);
-    case ED_F32: return step_typed<float, false>(s, w, v, vprev, vnext, scal, partials, st);
-    default: return step_typed<float, true>(s, w, v, vprev, vnext, scal, partials, st);
+    case ED_F64: return step_hv_typed<double, false>(s, w, v, vprev, vnext, scal, partials, st);
+    case ED_C128: return step_hv_typed<double, true>(s, w, v, vprev, vnext, scal, partials, st);
+    case ED_F32: return step_hv_typed<float, false>(s, w, v, vprev, vnext, scal, partials, st);
+    default: return step_hv_typed<float, true>(s, w, v, vprev, vnext, scal, partials, st);
     }
+}
+
+int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st) {
+    if (!dtype_ok(s, dtype)) return set_error(ED_ERR_INVALID, "ed_lanczos_update: dtype does not match the sector");
+    if (s.view.n == 0) return ED_OK;
+    switch (dtype) {
+    case ED_F64: return step_update_typed<double, false>(s, v, vnext, scal, st);
+    case ED_C128: return step_update_typed<double, true>(s, v, vnext, scal, st);
+    case ED_F32: return step_update_typed<float, false>(s, v, vnext, scal, st);
+    default: return step_update_typed<float, true>(s, v, vnext, scal, st);
+    }
+}
+
+int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
+                        double* scal, double* partials, cudaStream_t st) {
+    int rc = lanczos_hv_launch(s, w, dtype, v, vprev, vnext, scal, partials, st);
+    if (rc != ED_OK) return rc;
+    return lanczos_update_launch(s, dtype, v, vnext, scal, st);
+}
+
+template <typename R, bool CPLX>
+__global__ void accumulate_kernel(int64_t n, const void* __restrict__ x, double cr, double ci, void* __restrict__ acc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        R xr, xi;
+        ld<R, CPLX>(x, i, xr, xi);
+        if constexpr (CPLX) {
+            double2* a = reinterpret_cast<double2*>(acc) + i;
+            double2 t = *a;
+            t.x += cr * (double)xr - ci * (double)xi;
+            t.y += cr * (double)xi + ci * (double)xr;
+            *a = t;
+        } else {
+            reinterpret_cast<double*>(acc)[i] += cr * (double)xr;
+        }
+    }
+}
+
+int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st) {
+    if (!dtype_ok(s, dtype)) return set_error(ED_ERR_INVALID, "ed_accumulate: dtype does not match the sector");
+    if (s.view.n == 0) return ED_OK;
+    const int g = grid_for(s.view.n, 256, s.num_sms, 16);
+    switch (dtype) {
+    case ED_F64: accumulate_kernel<double, false><<<g, 256, 0, st>>>(s.view.n, x, cr, ci, acc); break;
+    case ED_C128: accumulate_kernel<double, true><<<g, 256, 0, st>>>(s.view.n, x, cr, ci, acc); break;
+    case ED_F32: accumulate_kernel<float, false><<<g, 256, 0, st>>>(s.view.n, x, cr, ci, acc); break;
+    default: accumulate_kernel<float, true><<<g, 256, 0, st>>>(s.view.n, x, cr, ci, acc); break;
+    }
+    ED_CHECK_LAUNCH("accumulate_kernel");
+    return ED_OK;
 }
 
 template <typename R, bool CPLX>

@@ -100,6 +100,10 @@ struct HvWeights {
 int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st);
 int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev,
                         void* vnext, double* scal, double* partials, cudaStream_t st);
+int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
+                      double* scal, double* partials, cudaStream_t st);
+int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st);
+int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st);
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
 int cf_launch(const double* a, const double* b, int m, const double* omega, int W, double e0, double eta,
               double norm2, double* out, cudaStream_t st);

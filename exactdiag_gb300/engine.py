@@ -135,6 +135,31 @@ class DeviceSector:
                   self._lib.ed_lanczos_step(self._h, w, code, _ptr(v), _ptr(v_prev), _ptr(v_next),
                                             _ptr(scal), _stream_ptr()))
 
+    def lanczos_hv(self, weights, v: torch.Tensor, v_prev: torch.Tensor | None, v_next: torch.Tensor,
+                   scal: torch.Tensor) -> None:
+        """First half of a step (ed_lanczos_hv): v_next <- H v - b v_prev, scalars on the device."""
+        code = self._code(v)
+        w = nat.weights_array(weights_tuple(weights))
+        nat.check("ed_lanczos_hv",
+                  self._lib.ed_lanczos_hv(self._h, w, code, _ptr(v), _ptr(v_prev), _ptr(v_next), _ptr(scal),
+                                          _stream_ptr()))
+
+    def lanczos_update(self, v: torch.Tensor, v_next: torch.Tensor, scal: torch.Tensor) -> None:
+        """Second half of a step (ed_lanczos_update): v_next <- (v_next - a v) / b."""
+        code = self._code(v)
+        nat.check("ed_lanczos_update",
+                  self._lib.ed_lanczos_update(self._h, code, _ptr(v), _ptr(v_next), _ptr(scal), _stream_ptr()))
+
+    def accumulate(self, x: torch.Tensor, coef: complex, acc: torch.Tensor) -> None:
+        """acc += coef * x with acc float64 (real sectors) or complex128 (ed_accumulate)."""
+        code = self._code(x)
+        want = torch.float64 if self.is_real else torch.complex128
+        if acc.dtype != want or not acc.is_cuda or acc.numel() != self.n:
+            raise ValueError(f"acc must be a {want} CUDA tensor of length n")
+        c = complex(coef)
+        nat.check("ed_accumulate",
+                  self._lib.ed_accumulate(self._h, code, _ptr(x), c.real, c.imag, _ptr(acc), _stream_ptr()))
+
     def normalize(self, x: torch.Tensor, norm_out: torch.Tensor) -> None:
         code = self._code(x)
         nat.check("ed_normalize", self._lib.ed_normalize(self._h, code, _ptr(x), _ptr(norm_out), _stream_ptr()))

@@ -35,13 +35,15 @@ class LanczosRun:
         self.norm = torch.zeros(1, dtype=torch.float64, device=dev)
         self.graph = None
 
-    def _record(self) -> None:
+    def _record(self, ritz=None, acc=None) -> None:
         s = self.sector
         s.normalize(self.buf[0], self.norm)
         self.scal.zero_()
         for k in range(self.m):
             v = self.buf[k % 2]
             other = self.buf[(k + 1) % 2]
+            if ritz is not None and k < len(ritz):
+                s.accumulate(v, ritz[k], acc)
             s.lanczos_step(self.weights, v, other if k > 0 else None, other, self.scal[2 * k: 2 * k + 4])
 
     def run(self, v0: torch.Tensor, use_graph: bool = True) -> None:
@@ -76,6 +78,54 @@ class LanczosRun:
     def last_vectors(self) -> tuple[torch.Tensor, torch.Tensor]:
         """(v_m, v_{m-1}) after a run of m steps (v_m normalised unless breakdown)."""
         return self.buf[self.m % 2], self.buf[(self.m + 1) % 2]
+
+
+def ritz_vector(run: LanczosRun, v0: torch.Tensor, coeffs: np.ndarray) -> torch.Tensor:
+    """sum_k coeffs[k] v_k in FP64, regenerating v_k by a second, bitwise-identical run from v0."""
+    sec = run.sector
+    acc = torch.zeros(sec.n, dtype=torch.float64 if sec.is_real else torch.complex128, device=sec.device)
+    run.buf[0].copy_(v0)
+    run._record(ritz=[complex(c) for c in coeffs], acc=acc)
+    return acc
+
+
+def ground_state(sector: DeviceSector, weights, num_steps: int, precision: str = "mixed", seed: int = 0,
+                 refine_steps: int = 12, v0: torch.Tensor | None = None, use_graph: bool = True) -> dict:
+    """Ground energy of a sector.
+
+    precision "fp64": plain FP64 Lanczos; E0 = lowest Ritz value.
+    precision "mixed": FP32 (complex64) Lanczos vectors with FP64 reductions;
+    the lowest Ritz vector is rebuilt in FP64 on a second pass and refined by
+    `refine_steps` FP64 Lanczos steps started from it (Rayleigh quotient and
+    residual come from that refinement run).
+    """
+    from scipy.linalg import eigh_tridiagonal
+
+    dt = sector.dtype("fp64" if precision == "fp64" else "fp32")
+    if v0 is None:
+        x = np.random.default_rng(seed).uniform(-1, 1, sector.n)
+        v0 = torch.as_tensor(x, device=sector.device).to(dt)
+    else:
+        v0 = v0.to(device=sector.device, dtype=dt)
+    run = LanczosRun(sector, weights, num_steps, dt)
+    run.run(v0, use_graph=use_graph)
+    a, b, _ = run.coefficients()
+    if len(a) == 1:
+        theta, vecs = np.array([a[0]]), np.ones((1, 1))
+    else:
+        theta, vecs = eigh_tridiagonal(a, b[1:])
+    out = {"theta": float(theta[0]), "a": a, "b": b, "steps": len(a), "E0": float(theta[0])}
+    if precision == "fp64":
+        return out
+    psi = ritz_vector(run, v0, vecs[:, 0])
+    ref = LanczosRun(sector, weights, refine_steps, psi.dtype)
+    ref.run(psi, use_graph=False)
+    ra, rb, _ = ref.coefficients()
+    rq = float(ra[0])
+    resid = float(rb[1]) if len(rb) > 1 else 0.0
+    e_ref = float(tridiagonal_eigvals(ra, rb)[0])
+    out.update({"E0": e_ref, "rayleigh": rq, "residual": resid, "refine_steps": len(ra)})
+    return out
 
 
 def lanczos_coefficients(sector: DeviceSector, weights, v0: torch.Tensor, num_lanczos_vecs: int,

@@ -84,6 +84,20 @@ int ed_hv(const ed_sector* s, const double weights[4], int dtype, const void* x_
 int ed_lanczos_step(const ed_sector* s, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
                     void* v_next_dev, double* scal_dev, void* stream);
 
+/* The two halves of ed_lanczos_step, for callers that time or interleave them:
+ * ed_lanczos_hv writes y = H v - b_k v_prev into v_next_dev and a_k, b_{k+1} into
+ * scal_dev[1..3]; ed_lanczos_update then forms v_{k+1} = (y - a_k v) / b_{k+1} in place. */
+int ed_lanczos_hv(const ed_sector* s, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
+                  void* v_next_dev, double* scal_dev, void* stream);
+int ed_lanczos_update(const ed_sector* s, int dtype, const void* v_dev, void* v_next_dev, const double* scal_dev,
+                      void* stream);
+
+/* acc += (coef_re + i coef_im) * x, with acc in FP64 (double for real dtypes,
+ * interleaved complex double otherwise) and x of the given dtype.  Builds Ritz
+ * vectors sum_k s_k v_k of a Lanczos run in FP64 (the refinement input). */
+int ed_accumulate(const ed_sector* s, int dtype, const void* x_dev, double coef_re, double coef_im, void* acc_dev,
+                  void* stream);
+
 /* Scales x in place to unit norm (FP64 accumulation); norm written to norm_dev[0]. */
 int ed_normalize(const ed_sector* s, int dtype, void* x_dev, double* norm_dev, void* stream);
 

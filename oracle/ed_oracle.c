@@ -707,3 +707,75 @@ int or_num_threads(void) {
     return 1;
 #endif
 }
+
+/* Full columns (both triangles) of one term for a subset of column indices:
+ * the sample used by the timed CPU baseline.  Same rule as or_term_columns. */
+int or_term_columns_subset(int L, int Nh, int Nd, int kx, int ky, int term, int triangle, const int64_t *d2s,
+                           const int32_t *orb, int64_t n, const int64_t *cols, int64_t ncols, int64_t *colptr,
+                           int64_t *rows, double *vre, double *vim, int64_t cap, int64_t *nnz_out) {
+    ors_t s;
+    if (sector_init(&s, L, Nh, Nd, kx, ky) != OR_OK || term < 0 || term > 3) return OR_EINVAL;
+    combos_t c;
+    term_combos(s.N, term, &c);
+    rule_t r = {&c, term < 2 ? VAL_HOLE_HOP : VAL_SPIN_SWAP, NEW_SWAP, term < 2, 0, triangle, &s, d2s, n};
+    int64_t *cnt = (int64_t *)calloc((size_t)ncols + 1, sizeof(int64_t));
+    if (!cnt) return OR_ENOMEM;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = 0; k < ncols; ++k) {
+        double complex vals[4 * OR_MAXN + 2];
+        int64_t inds[4 * OR_MAXN + 2];
+        int64_t i = cols[k];
+        cnt[k + 1] = column(&s, i, d2s[i], orb[i], &r, vals, inds);
+    }
+    for (int64_t k = 0; k < ncols; ++k) cnt[k + 1] += cnt[k];
+    *nnz_out = cnt[ncols];
+    if (colptr) memcpy(colptr, cnt, ((size_t)ncols + 1) * sizeof(int64_t));
+    if (!rows) {
+        free(cnt);
+        return OR_OK;
+    }
+    if (cnt[ncols] > cap) {
+        free(cnt);
+        return OR_ECAP;
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = 0; k < ncols; ++k) {
+        double complex vals[4 * OR_MAXN + 2];
+        int64_t inds[4 * OR_MAXN + 2];
+        int64_t i = cols[k];
+        int m = column(&s, i, d2s[i], orb[i], &r, vals, inds);
+        for (int q = 0; q < m; ++q) {
+            rows[cnt[k] + q] = inds[q];
+            vre[cnt[k] + q] = creal(vals[q]);
+            vim[cnt[k] + q] = cimag(vals[q]);
+        }
+    }
+    free(cnt);
+    return OR_OK;
+}
+
+/* The reference's SpMV over its row-major Hermitian-triangle storage, for a
+ * set of stored rows (general/cpp_sparse_dot.h:59-71 explicit pass and
+ * :104-138 Hermitian-conjugate pass, driven as in
+ * general/cython_sparse_dot.pyx:65-79 with num_threads = 1): row r holds the
+ * entries (col >= r, value index) of U; y[r] += w * sum U[r,c] x[c] and
+ * y[c] += w * x[r] * conj(U[r,c]) for c != r.  Single-threaded like the
+ * reference's only race-free setting. */
+void or_spmv_triangle_rows(int64_t nrows, const int64_t *row_ids, const int64_t *ptr, const int64_t *cols,
+                           const int16_t *vidx, const double complex *vals, const double complex *x,
+                           double complex *y, double w_re, double w_im) {
+    const double complex w = w_re + I * w_im;
+    for (int64_t k = 0; k < nrows; ++k) {
+        double complex acc = 0;
+        for (int64_t j = ptr[k]; j < ptr[k + 1]; ++j) acc += x[cols[j]] * vals[vidx[j]];
+        y[row_ids[k]] += w * acc;
+    }
+    for (int64_t k = 0; k < nrows; ++k) {
+        const int64_t r = row_ids[k];
+        for (int64_t j = ptr[k]; j < ptr[k + 1]; ++j) {
+            const int64_t c = cols[j];
+            if (c == r) continue;
+            y[c] += x[r] * conj(vals[vidx[j]]) * w;
+        }
+    }
+}

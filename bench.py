@@ -40,6 +40,7 @@ METRIC = "Lanczos steps/s & HÂ·v HBM GB/s, 2Ã—14 t-J: mixed vs FP64 GPU at Î”Eâ‰
 UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
+KERNEL_VERSION = "v1"  # the H.v kernel generation the committed traffic figure was captured on
 WORKLOAD = "2x14 t-J ladder, 2 holes, Sz=0, k=(0,0), t=1, J=0.5: fused Lanczos step over the full sector"
 
 
@@ -109,13 +110,17 @@ class ClockSampler:
 
 def ncu_traffic(workload_key: str) -> float | None:
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if it covers this workload."""
-    p = ROOT / "profiles" / "lanczos_hv_2x14_traffic.json"
+    p = ROOT / "profiles" / "lanczos_hv_2x14_traffic.txt"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    if d.get("workload") != workload_key:
+    fields = {}
+    for line in p.read_text().splitlines():
+        if ":" in line and not line.startswith("#"):
+            k, v = line.split(":", 1)
+            fields[k.strip()] = v.strip()
+    if fields.get("workload") != workload_key or fields.get("kernel_version") != KERNEL_VERSION:
         return None
-    return float(d["dram_bytes_per_launch"])
+    return float(fields["dram_bytes_per_launch"])
 
 
 # ----------------------------------------------------------------------------- engine arm

@@ -44,6 +44,10 @@ SIGNATURES = {
     "ed_normalize": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp]),
     "ed_continued_fraction": (_c.c_int, [_vp, _vp, _c.c_int, _vp, _c.c_int, _c.c_double, _c.c_double, _c.c_double,
                                          _vp, _vp]),
+    "ed_excitation_apply": (_c.c_int, [_vp, _vp, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _vp, _vp, _vp]),
+    "ed_batch_lanczos": (_c.c_int, [_c.POINTER(_vp), _c.c_int, _d4, _c.c_int, _c.POINTER(_vp), _c.c_int, _vp,
+                                    _c.c_int, _vp]),
+    "ed_project_out": (_c.c_int, [_vp, _c.c_int, _vp, _c.c_int, _vp, _vp, _vp]),
     "ed_last_error_string": (_c.c_char_p, []),
 }
 

@@ -25,7 +25,7 @@ int set_cuda_error(cudaError_t e, const char* what) {
     return ED_ERR_CUDA;
 }
 
-size_t hv_smem_bytes(const SectorView& S, size_t real_size);
+size_t hv_smem_bytes_host(const SectorView& S, size_t real_size);
 int hv_blocks_per_sm(const SectorView& S);
 
 static void host_comb(uint32_t c[kCombStride][kCombStride]) {
@@ -223,6 +223,45 @@ int ed_normalize(const ed_sector* h, int dtype, void* x_dev, double* norm_dev, v
     if (!h || !x_dev || !norm_dev) return set_error(ED_ERR_INVALID, "ed_normalize: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_normalize: basis not built");
     return normalize_launch(h->s, dtype, x_dev, norm_dev, h->s.d_partials.p, (cudaStream_t)stream);
+}
+
+int ed_excitation_apply(const ed_sector* src, const ed_sector* dst, int op, int qx, int qy, int initial_sz2, int dtype,
+                        const void* x_src_dev, void* y_dst_dev, void* stream) {
+    if (!src || !dst || !x_src_dev || !y_dst_dev) return set_error(ED_ERR_INVALID, "ed_excitation_apply: NULL");
+    if (!src->s.built || !dst->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_excitation_apply: basis not built");
+    return excite_launch(src->s, dst->s, op, qx, qy, initial_sz2, dtype, x_src_dev, y_dst_dev, (cudaStream_t)stream);
+}
+
+int ed_batch_lanczos(const ed_sector* const* sectors, int nsec, const double weights[4], int dtype,
+                     const void* const* v0_dev, int m, double* coef_dev, int use_graph, void* stream) {
+    if (!sectors || nsec <= 0 || !v0_dev || !coef_dev) return set_error(ED_ERR_INVALID, "ed_batch_lanczos: NULL");
+    HvWeights w;
+    if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_batch_lanczos: weights");
+    std::vector<const Sector*> secs;
+    for (int i = 0; i < nsec; ++i) {
+        if (!sectors[i] || !v0_dev[i]) return set_error(ED_ERR_INVALID, "ed_batch_lanczos: NULL sector or vector");
+        secs.push_back(&sectors[i]->s);
+    }
+    try {
+        return batch_lanczos_launch(secs, w, dtype, v0_dev, m, coef_dev, use_graph, (cudaStream_t)stream);
+    } catch (...) {
+        return set_error(ED_ERR_INTERNAL, "ed_batch_lanczos: exception");
+    }
+}
+
+int ed_project_out(ed_sector* h, int dtype, const void* basis_dev, int k, void* w_dev, double* coef_dev,
+                   void* stream) {
+    if (!h || !basis_dev || !w_dev || k < 0) return set_error(ED_ERR_INVALID, "ed_project_out: bad argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_project_out: basis not built");
+    if (k == 0) return ED_OK;
+    Sector& s = h->s;
+    const int64_t need = (int64_t)k * 2 * s.num_sms * kReduceSlots + 2 * (int64_t)k;
+    if (s.d_proj.n < need) {
+        cudaStreamSynchronize((cudaStream_t)stream);
+        if (!s.d_proj.alloc(need)) return set_error(ED_ERR_NOMEM, "ed_project_out: scratch");
+    }
+    return project_launch(s, dtype, basis_dev, k, w_dev, coef_dev ? coef_dev : s.d_proj.p, s.d_proj.p + 2 * k,
+                          s.d_proj.n - 2 * k, (cudaStream_t)stream);
 }
 
 int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const double* omega_dev, int W, double e0,

@@ -1,0 +1,372 @@
+// ed_batch.cu -- several Lanczos recursions at once, and Gram-Schmidt projection.
+//
+// Batched recursion: the target sectors of a dynamical spectrum (all momenta q
+// and rung parities, uneven dimensions; tJ_spin_half_ladder/api.py:116-161
+// loops over them one at a time, each through
+// general/cython_lanczos_diagonalization.pyx:50-77) run together.  The rows of
+// all sectors are cut into chunks; each phase of a step is one launch over all
+// chunks (fused H.v with per-chunk FP64 partial sums, per-sector scalars, the
+// in-place update), and the m steps are captured once into a CUDA graph that is
+// launched once.  The sectors of one batch share L, Nh and Nd (one set of
+// shared-memory tables); they differ in momentum and dimension.
+//
+// Projection (full reorthogonalisation for the lowest-eigenpair solver):
+// w <- w - sum_j <v_j, w> v_j with FP64 dot products.
+#include <vector>
+
+#include "ed_device.cuh"
+
+namespace ed {
+
+struct BatchChunk {
+    int32_t sec;
+    int32_t pad;
+    int64_t begin, end;  // rows of sector `sec`
+};
+
+constexpr int kChunkRows = 1 << 16;
+
+__device__ __forceinline__ void chunk_reduce(double v[kReduceSlots], double* __restrict__ out) {
+    __shared__ double red[kReduceSlots][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kReduceSlots; ++k) {
+        double t = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) red[k][wid] = t;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < kReduceSlots; ++k) {
+            double t = lane < nw ? red[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+            if (lane == 0) out[k] = t;
+        }
+    }
+    __syncthreads();
+}
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void* vec_at(void* base, int64_t off) {
+    return reinterpret_cast<typename Vec<R, CPLX>::T*>(base) + off;
+}
+
+template <typename R, bool CPLX>
+__global__ void __launch_bounds__(kHvThreads)
+    batch_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
+                    const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* other, int first,
+                    const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const HvTables<R> tb = load_tables<R>(views[0], smem);
+    const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const BatchChunk ch = chunks[c];
+        const SectorView S = views[ch.sec];
+        const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
+        void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
+        const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
+        double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
+        for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
+            R hr, hi, xr, xi;
+            hv_row<R, CPLX>(S, tb, w, i, x, hr, hi, xr, xi);
+            R yr = hr, yi = hi;
+            if (!first) {
+                R pr, pi;
+                ld<R, CPLX>(y, i, pr, pi);  // y holds v_{k-1} before it is overwritten by this row
+                yr -= beta * pr;
+                yi -= beta * pi;
+            }
+            st<R, CPLX>(y, i, yr, yi);
+            const double dxr = xr, dxi = xi, dyr = yr, dyi = yi;
+            acc[0] = fma(dxr, (double)hr, fma(dxi, (double)hi, acc[0]));
+            acc[1] = fma(dyr, dyr, fma(dyi, dyi, acc[1]));
+            acc[2] = fma(dxr, dyr, fma(dxi, dyi, acc[2]));
+            acc[3] = fma(dxr, dxr, fma(dxi, dxi, acc[3]));
+        }
+        chunk_reduce(acc, partials + (int64_t)c * kReduceSlots);
+    }
+}
+
+// One CTA per sector: a_k, b_{k+1} from the sector's chunk partials (fixed order).
+__global__ void batch_scalars_kernel(const double* __restrict__ partials, const int* __restrict__ cfirst,
+                                     const int* __restrict__ ccount, double* __restrict__ scal, int stride, int k,
+                                     int norm_mode) {
+    __shared__ double red[kReduceSlots][32];
+    const int s = blockIdx.x;
+    double t[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = threadIdx.x; c < ccount[s]; c += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < kReduceSlots; ++q) t[q] += partials[(int64_t)(cfirst[s] + c) * kReduceSlots + q];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kReduceSlots; ++q) {
+        double v = t[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[q][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot[kReduceSlots];
+        for (int q = 0; q < kReduceSlots; ++q) {
+            tot[q] = 0.0;
+            for (int i = 0; i < nw; ++i) tot[q] += red[q][i];
+        }
+        double* X = scal + (int64_t)s * stride;
+        if (norm_mode) {
+            X[stride - 1] = sqrt(tot[3]);  // |v0|
+            return;
+        }
+        const double a = tot[0];
+        const double nn = tot[1] - 2.0 * a * tot[2] + a * a * tot[3];
+        const double b = sqrt(nn > 0.0 ? nn : 0.0);
+        X[2 * k + 1] = a;
+        X[2 * k + 2] = b;
+        X[2 * k + 3] = (b < 1e-8) ? 1.0 : 0.0;
+    }
+}
+
+template <typename R, bool CPLX>
+__global__ void batch_norm_partials_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+                                           int nchunks, const void* v, double* __restrict__ partials) {
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const BatchChunk ch = chunks[c];
+        const void* x = vec_at<R, CPLX>(const_cast<void*>(v), offs[ch.sec]);
+        double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
+        for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
+            R xr, xi;
+            ld<R, CPLX>(x, i, xr, xi);
+            acc[3] = fma((double)xr, (double)xr, fma((double)xi, (double)xi, acc[3]));
+        }
+        chunk_reduce(acc, partials + (int64_t)c * kReduceSlots);
+    }
+}
+
+// mode 0: v_next = (y - a v) / b (step update); mode 1: v *= 1/|v0| (start vector)
+template <typename R, bool CPLX>
+__global__ void batch_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+                                    int nchunks, void* v, void* other, const double* __restrict__ scal, int stride,
+                                    int k, int mode) {
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const BatchChunk ch = chunks[c];
+        const double* X = scal + (int64_t)ch.sec * stride;
+        void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
+        if (mode == 1) {
+            const double nv = X[stride - 1];
+            const R inv = nv > 0.0 ? (R)(1.0 / nv) : R(0);
+            for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
+                R xr, xi;
+                ld<R, CPLX>(x, i, xr, xi);
+                st<R, CPLX>(x, i, xr * inv, xi * inv);
+            }
+            continue;
+        }
+        void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
+        const R a = (R)X[2 * k + 1];
+        const bool brk = X[2 * k + 3] != 0.0;
+        const R inv = brk ? R(1) : (R)(1.0 / X[2 * k + 2]);
+        for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
+            R vr, vi, yr, yi;
+            ld<R, CPLX>(x, i, vr, vi);
+            ld<R, CPLX>(y, i, yr, yi);
+            st<R, CPLX>(y, i, (yr - a * vr) * inv, (yi - a * vi) * inv);
+        }
+    }
+}
+
+template <typename R, bool CPLX>
+static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& w, const void* const* v0, int m,
+                       double* coef, int use_graph, cudaStream_t st) {
+    const int nsec = (int)secs.size();
+    const size_t esz = sizeof(typename Vec<R, CPLX>::T);
+    std::vector<SectorView> hviews(nsec);
+    std::vector<int64_t> hoffs(nsec);
+    std::vector<BatchChunk> hchunks;
+    std::vector<int> cfirst(nsec), ccount(nsec);
+    int64_t total = 0;
+    for (int s = 0; s < nsec; ++s) {
+        hviews[s] = secs[s]->view;
+        hoffs[s] = total;
+        cfirst[s] = (int)hchunks.size();
+        for (int64_t b = 0; b < hviews[s].n; b += kChunkRows) {
+            BatchChunk c{};
+            c.sec = s;
+            c.begin = b;
+            c.end = std::min<int64_t>(hviews[s].n, b + kChunkRows);
+            hchunks.push_back(c);
+        }
+        ccount[s] = (int)hchunks.size() - cfirst[s];
+        total += hviews[s].n;
+    }
+    const int nchunks = (int)hchunks.size();
+    const int stride = 2 * m + 4;
+    DevBuf<SectorView> dviews(nsec);
+    DevBuf<int64_t> doffs(nsec);
+    DevBuf<BatchChunk> dchunks(nchunks);
+    DevBuf<int> dcfirst(nsec), dccount(nsec);
+    DevBuf<double> partials((int64_t)nchunks * kReduceSlots);
+    DevBuf<uint8_t> buf0((int64_t)(total * esz)), buf1((int64_t)(total * esz));
+    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dcfirst.ok() || !dccount.ok() || !partials.ok() ||
+        !buf0.ok() || !buf1.ok())
+        return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
+    cudaMemcpyAsync(dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(doffs.p, hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dchunks.p, hchunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dcfirst.p, cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dccount.p, ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(coef, 0, (size_t)nsec * stride * sizeof(double), st);
+    for (int s = 0; s < nsec; ++s)
+        if (hviews[s].n)
+            cudaMemcpyAsync(buf0.p + hoffs[s] * esz, v0[s], hviews[s].n * esz, cudaMemcpyDeviceToDevice, st);
+    const int grid = std::min(nchunks, secs[0]->hv_grid > 0 ? secs[0]->hv_grid : secs[0]->num_sms * 3);
+    const size_t smem = hv_smem_bytes(hviews[0], sizeof(R));
+    cudaFuncSetAttribute(batch_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // start vectors: |v0| and normalisation
+    batch_norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
+    batch_scalars_kernel<<<nsec, 256, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1);
+    batch_update_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
+                                                       1);
+    ED_CHECK_LAUNCH("batch start vectors");
+    cudaStream_t cap = st;
+    cudaStream_t priv = nullptr;
+    if (use_graph) {
+        if (cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking) != cudaSuccess)
+            return set_error(ED_ERR_CUDA, "ed_batch_lanczos: stream");
+        cap = priv;
+        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaStreamDestroy(priv);
+            return set_error(ED_ERR_CUDA, "ed_batch_lanczos: begin capture");
+        }
+    }
+    uint8_t* b[2] = {buf0.p, buf1.p};
+    for (int k = 0; k < m; ++k) {
+        void* v = b[k % 2];
+        void* other = b[(k + 1) % 2];
+        batch_hv_kernel<R, CPLX><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
+                                                                  k == 0, coef, stride, k, partials.p);
+        batch_scalars_kernel<<<nsec, 256, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0);
+        batch_update_kernel<R, CPLX><<<grid, 256, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0);
+    }
+    if (use_graph) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(priv);
+        if (e != cudaSuccess) return set_cuda_error(e, "ed_batch_lanczos: graph");
+    } else {
+        ED_CHECK_LAUNCH("batch steps");
+        if (cudaStreamSynchronize(st) != cudaSuccess) return set_error(ED_ERR_CUDA, "ed_batch_lanczos: steps");
+    }
+    return ED_OK;
+}
+
+int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,
+                         int m, double* coef, int use_graph, cudaStream_t st) {
+    if (secs.empty() || m <= 0) return set_error(ED_ERR_INVALID, "ed_batch_lanczos: empty batch or m <= 0");
+    const SectorView& a = secs[0]->view;
+    for (const Sector* s : secs) {
+        if (!s->built) return set_error(ED_ERR_NOT_BUILT, "ed_batch_lanczos: basis not built");
+        if (s->view.L != a.L || s->view.Nh != a.Nh || s->view.Nd != a.Nd)
+            return set_error(ED_ERR_INVALID, "ed_batch_lanczos: sectors must share L, Nh and Nd");
+        if ((dtype == ED_F64 || dtype == ED_F32) && !s->real)
+            return set_error(ED_ERR_INVALID, "ed_batch_lanczos: real dtype with a complex sector");
+    }
+    switch (dtype) {
+    case ED_F64: return batch_typed<double, false>(secs, w, v0, m, coef, use_graph, st);
+    case ED_C128: return batch_typed<double, true>(secs, w, v0, m, coef, use_graph, st);
+    case ED_F32: return batch_typed<float, false>(secs, w, v0, m, coef, use_graph, st);
+    case ED_C64: return batch_typed<float, true>(secs, w, v0, m, coef, use_graph, st);
+    default: return set_error(ED_ERR_INVALID, "ed_batch_lanczos: dtype");
+    }
+}
+
+// ------------------------------------------------------------ projection
+
+template <typename R, bool CPLX>
+__global__ void proj_dots_kernel(int64_t n, const void* __restrict__ V, const void* __restrict__ w, int nchunks,
+                                 double* __restrict__ partials) {
+    const int j = blockIdx.y;
+    const int64_t per = (n + nchunks - 1) / nchunks;
+    const int64_t b = (int64_t)blockIdx.x * per, e = min(n, b + per);
+    double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
+    const typename Vec<R, CPLX>::T* vj = reinterpret_cast<const typename Vec<R, CPLX>::T*>(V) + (int64_t)j * n;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        R vr, vi, wr, wi;
+        ld<R, CPLX>(vj, i, vr, vi);
+        ld<R, CPLX>(w, i, wr, wi);
+        // conj(v) * w
+        acc[0] = fma((double)vr, (double)wr, fma((double)vi, (double)wi, acc[0]));
+        acc[1] = fma((double)vr, (double)wi, fma(-(double)vi, (double)wr, acc[1]));
+    }
+    chunk_reduce(acc, partials + ((int64_t)j * nchunks + blockIdx.x) * kReduceSlots);
+}
+
+__global__ void proj_coef_kernel(const double* __restrict__ partials, int nchunks, double* __restrict__ coef) {
+    const int j = blockIdx.x;
+    if (threadIdx.x == 0) {
+        double re = 0.0, im = 0.0;
+        for (int c = 0; c < nchunks; ++c) {
+            re += partials[((int64_t)j * nchunks + c) * kReduceSlots];
+            im += partials[((int64_t)j * nchunks + c) * kReduceSlots + 1];
+        }
+        coef[2 * j] = re;
+        coef[2 * j + 1] = im;
+    }
+}
+
+template <typename R, bool CPLX>
+__global__ void proj_sub_kernel(int64_t n, const void* __restrict__ V, int k, const double* __restrict__ coef,
+                                void* __restrict__ w) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        R wr0, wi0;
+        ld<R, CPLX>(w, i, wr0, wi0);
+        double wr = wr0, wi = wi0;
+        for (int j = 0; j < k; ++j) {
+            R vr, vi;
+            ld<R, CPLX>(reinterpret_cast<const typename Vec<R, CPLX>::T*>(V) + (int64_t)j * n, i, vr, vi);
+            const double cr = coef[2 * j], ci = coef[2 * j + 1];
+            wr -= cr * (double)vr - ci * (double)vi;
+            wi -= cr * (double)vi + ci * (double)vr;
+        }
+        st<R, CPLX>(w, i, (R)wr, (R)wi);
+    }
+}
+
+template <typename R, bool CPLX>
+static int project_typed(const Sector& s, const void* V, int k, void* w, double* coef, double* partials,
+                         int nchunks, cudaStream_t st) {
+    const int64_t n = s.view.n;
+    dim3 g(nchunks, k);
+    proj_dots_kernel<R, CPLX><<<g, 256, 0, st>>>(n, V, w, nchunks, partials);
+    proj_coef_kernel<<<k, 32, 0, st>>>(partials, nchunks, coef);
+    proj_sub_kernel<R, CPLX><<<grid_for(n, 256, s.num_sms, 16), 256, 0, st>>>(n, V, k, coef, w);
+    ED_CHECK_LAUNCH("projection kernels");
+    return ED_OK;
+}
+
+int project_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef, double* scratch,
+                   int64_t scratch_len, cudaStream_t st) {
+    if (k <= 0 || s.view.n == 0) return ED_OK;
+    int nchunks = (int)std::min<int64_t>(2 * s.num_sms, (s.view.n + 1023) / 1024);
+    if (nchunks < 1) nchunks = 1;
+    if ((int64_t)k * nchunks * kReduceSlots > scratch_len) nchunks = (int)(scratch_len / ((int64_t)k * kReduceSlots));
+    if (nchunks < 1) return set_error(ED_ERR_TOO_LARGE, "ed_project_out: scratch too small for k vectors");
+    if (k > 65535) return set_error(ED_ERR_TOO_LARGE, "ed_project_out: k too large");
+    switch (dtype) {
+    case ED_F64: return project_typed<double, false>(s, V, k, w, coef, scratch, nchunks, st);
+    case ED_C128: return project_typed<double, true>(s, V, k, w, coef, scratch, nchunks, st);
+    case ED_F32: return project_typed<float, false>(s, V, k, w, coef, scratch, nchunks, st);
+    case ED_C64: return project_typed<float, true>(s, V, k, w, coef, scratch, nchunks, st);
+    default: return set_error(ED_ERR_INVALID, "ed_project_out: dtype");
+    }
+}
+
+}  // namespace ed

@@ -1,0 +1,251 @@
+// ed_device.cuh -- device-side pieces shared by the row kernels: shared-memory
+// tables, typed vector access, the representative lookup and the H.v row.
+#pragma once
+#include "ed_internal.cuh"
+
+namespace ed {
+
+template <typename R>
+struct HvTables {
+    const uint32_t* rank;  // shared
+    const uint32_t* comb;  // shared
+    const R* cosv;         // cos(pi e / L), e in [0, 2L)
+    const R* sinv;         // +sin(pi e / L): conj(u^e) = cos + i sin
+    const R* sqrtv;        // sqrt(k), k in [0, 32]
+    const R* rsqrtv;       // 1/sqrt(k)
+};
+
+template <typename R, bool CPLX>
+struct Vec;
+template <>
+struct Vec<float, false> {
+    using T = float;
+};
+template <>
+struct Vec<float, true> {
+    using T = float2;
+};
+template <>
+struct Vec<double, false> {
+    using T = double;
+};
+template <>
+struct Vec<double, true> {
+    using T = double2;
+};
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void ld(const void* v, int64_t j, R& re, R& im) {
+    using T = typename Vec<R, CPLX>::T;
+    const T t = __ldg(reinterpret_cast<const T*>(v) + j);
+    if constexpr (CPLX) {
+        re = t.x;
+        im = t.y;
+    } else {
+        re = t;
+        im = R(0);
+    }
+}
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void st(void* v, int64_t j, R re, R im) {
+    using T = typename Vec<R, CPLX>::T;
+    if constexpr (CPLX) {
+        T t;
+        t.x = re;
+        t.y = im;
+        reinterpret_cast<T*>(v)[j] = t;
+    } else {
+        reinterpret_cast<T*>(v)[j] = re;
+    }
+}
+
+// Dense row of representative spin mask `dr` in block B, or -1 when the
+// configuration is not a representative of the sector.
+__device__ __forceinline__ int64_t dense_in_block(const SectorView& S, const BlockInfo& B, uint32_t dr,
+                                                  const uint32_t* rank_tab) {
+    const uint32_t r = spin_rank(compress_spins(dr, B.hmask), rank_tab, S.Nd);
+    if (B.flags & kBlockFree) return B.start + (int64_t)r;
+    const int64_t w = B.word_off + (r >> 6);
+    const uint64_t bits = S.bitmap[w];
+    const uint64_t bit = 1ull << (r & 63u);
+    if (!(bits & bit)) return -1;
+    return S.word_prefix[w] + __popcll(bits & (bit - 1ull));
+}
+
+struct Resolved {
+    int64_t j;  // dense row of the representative, -1 if absent or incompatible
+    int nj;     // orbit size of the new state
+    int e;      // phase exponent (units of pi/L) of its lowest image
+};
+
+// Representative of the configuration (h2, d2) in sector S: dense row, orbit
+// size and phase exponent of the lowest image
+// (general/symmetry.h:97-126 then general/basis_indexing.h:152-168).
+__device__ __forceinline__ Resolved resolve(const SectorView& S, const uint32_t* rank_tab, const uint32_t* comb,
+                                            uint32_t h2, uint32_t d2) {
+    const HoleEntry he = S.holes[hole_rank(h2, comb)];
+    if (he.block < 0) return {-1, 0, 0};
+    const BlockInfo B = S.blocks[he.block];
+    int nj, e;
+    uint32_t dr;
+    if (he.free_) {
+        uint32_t hh = h2;
+        dr = d2;
+        apply_p(he.p_star, hh, dr, S.N, S.mask);
+        nj = S.N;
+        e = he.e_star;
+    } else {
+        const OrbitResult o = orbit_walk(S.L, S.kx, S.ky, S.ne_even, S.mask, h2, d2, false);
+        if (o.found == 0) return {-1, 0, 0};
+        dr = (uint32_t)o.low;
+        nj = o.found;
+        e = o.e;
+    }
+    return {dense_in_block(S, B, dr, rank_tab), nj, e};
+}
+
+// Accumulate conj(M[j,i]) x_j for the new state (h2, d2); `coef` already holds
+// w_t * c_t * sign_F * sqrt(N_i).
+template <typename R, bool CPLX>
+__device__ __forceinline__ void add_target(const SectorView& S, const HvTables<R>& tb, uint32_t h2, uint32_t d2, R coef,
+                                           const void* __restrict__ x, R& accr, R& acci) {
+    const Resolved rv = resolve(S, tb.rank, tb.comb, h2, d2);
+    const int64_t j = rv.j;
+    if (j < 0) return;
+    const int nj = rv.nj, e = rv.e;
+    const R c = coef * tb.rsqrtv[nj];
+    R xr, xi;
+    ld<R, CPLX>(x, j, xr, xi);
+    if constexpr (CPLX) {
+        const R pr = c * tb.cosv[e], pi = c * tb.sinv[e];
+        accr += pr * xr - pi * xi;
+        acci += pr * xi + pi * xr;
+    } else {
+        accr += (e == 0 ? c : -c) * xr;
+    }
+}
+
+// Row i of H applied to x.  Returns (re, im) of (Hx)_i.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void hv_row(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
+                                       const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
+    const uint64_t key = S.keys[i];
+    const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
+    const int N = S.N;
+    const uint32_t mask = S.mask;
+    const uint32_t occ = ~h & mask;
+    const R sqNi = tb.sqrtv[S.orbit[i]];
+    const HoleEntry hrow = S.holes[hole_rank(h, tb.comb)];
+    const BlockInfo Brow = S.blocks[hrow.block];
+    const bool row_free = hrow.free_;
+    R accr = R(0), acci = R(0), diag = R(0);
+    ld<R, CPLX>(x, i, xir, xii);
+
+    // exchange: jl (leg bonds a -- a+2), jr (rung bonds 2x -- 2x+1)
+#pragma unroll
+    for (int t = 2; t < 4; ++t) {
+        const R wt = w[t];
+        if (wt == R(0)) continue;
+        uint32_t m;
+        int step;
+        if (t == 2) {
+            const uint32_t occ2 = rotl_n(occ, N - 2, N, mask), d2r = rotl_n(d, N - 2, N, mask);
+            m = occ & occ2 & (d ^ d2r);
+            step = 2;
+        } else {
+            m = occ & (occ >> 1) & (d ^ (d >> 1)) & 0x55555555u & mask;
+            step = 1;
+        }
+        diag += R(-0.5) * wt * (R)__popc(m);
+        const R coef = R(0.5) * wt * sqNi;
+        while (m) {
+            const int a = __ffs(m) - 1;
+            m &= m - 1u;
+            int b = a + step;
+            if (b >= N) b -= N;
+            const uint32_t d2 = d ^ (1u << a) ^ (1u << b);
+            if (row_free) {
+                // the row's hole mask is canonical with a trivial stabiliser: the new
+                // state is its own representative, orbit 2L, phase 1.
+                const int64_t j = Brow.start + (int64_t)spin_rank(compress_spins(d2, h), tb.rank, S.Nd);
+                R xr, xi;
+                ld<R, CPLX>(x, j, xr, xi);
+                const R c = coef * tb.rsqrtv[N];
+                accr += c * xr;
+                if constexpr (CPLX) acci += c * xi;
+            } else {
+                add_target<R, CPLX>(S, tb, h, d2, coef, x, accr, acci);
+            }
+        }
+    }
+    // hopping: tl (a -> a +- 2 along the leg), tr (across the rung)
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const R wt = w[t];
+        if (wt == R(0)) continue;
+        const R coef = -wt * sqNi;
+#pragma unroll
+        for (int dir = 0; dir < 2; ++dir) {
+            uint32_t m;
+            if (t == 0) {
+                // electron at a, hole at a+2 (dir 0) or a-2 (dir 1)
+                m = occ & (dir == 0 ? rotl_n(h, N - 2, N, mask) : rotl_n(h, 2 % N, N, mask));
+            } else {
+                m = dir == 0 ? (occ & (h >> 1) & 0x55555555u) : (occ & (h << 1) & 0xAAAAAAAAu & mask);
+            }
+            while (m) {
+                const int a = __ffs(m) - 1;
+                m &= m - 1u;
+                int b;
+                if (t == 0) {
+                    b = dir == 0 ? a + 2 : a - 2;
+                    if (b >= N) b -= N;
+                    if (b < 0) b += N;
+                } else {
+                    b = dir == 0 ? a + 1 : a - 1;
+                }
+                const int lo = min(a, b), hi = max(a, b);
+                const uint32_t between = ((1u << hi) - 1u) & ~((2u << lo) - 1u);
+                const int sgn = (__popc(occ & between) & 1) ? -1 : 1;
+                const uint32_t h2 = h ^ (1u << a) ^ (1u << b);
+                const uint32_t d2 = ((d >> a) & 1u) ? (d ^ (1u << a) ^ (1u << b)) : d;
+                add_target<R, CPLX>(S, tb, h2, d2, sgn > 0 ? coef : -coef, x, accr, acci);
+            }
+        }
+    }
+    outr = accr + diag * xir;
+    outi = acci + diag * xii;
+}
+
+template <typename R>
+__device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
+    uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem);
+    const int tab_words = 4 * (S.Nd + 1) * 256;
+    uint32_t* s_comb = s_rank + tab_words;
+    R* s_f = reinterpret_cast<R*>(s_comb + kCombStride * kCombStride + 1);  // 8-byte aligned (odd count + 1)
+    R* s_cos = s_f;
+    R* s_sin = s_f + 64;
+    R* s_sqrt = s_f + 128;
+    R* s_rsqrt = s_f + 161;
+    for (int i = threadIdx.x; i < tab_words; i += blockDim.x) s_rank[i] = S.rank_tab[i];
+    for (int i = threadIdx.x; i < kCombStride * kCombStride; i += blockDim.x) s_comb[i] = S.comb[i];
+    for (int i = threadIdx.x; i < 2 * S.L; i += blockDim.x) {
+        double c, s;
+        sincospi((double)i / (double)S.L, &s, &c);
+        s_cos[i] = (R)c;
+        s_sin[i] = (R)s;
+    }
+    for (int i = threadIdx.x; i <= kMaxN; i += blockDim.x) {
+        s_sqrt[i] = (R)sqrt((double)i);
+        s_rsqrt[i] = i ? (R)(1.0 / sqrt((double)i)) : R(0);
+    }
+    __syncthreads();
+    return HvTables<R>{s_rank, s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
+}
+
+inline size_t hv_smem_bytes(const SectorView& S, size_t real_size) {
+    return (4 * (S.Nd + 1) * 256 + kCombStride * kCombStride + 1) * sizeof(uint32_t) + (64 + 64 + 33 + 33) * real_size;
+}
+
+}  // namespace ed

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "../../include/exactdiag_gb300.h"
 #include "ed_common.cuh"
@@ -83,6 +84,7 @@ struct Sector {
     DevBuf<uint64_t> d_keys;
     DevBuf<uint8_t> d_orbit;
     DevBuf<double> d_partials;   // [hv_grid][kReduceSlots] scratch of the fused Lanczos step
+    DevBuf<double> d_proj;       // projection scratch: partial dots and coefficients
 };
 
 // ed_basis.cu
@@ -105,6 +107,12 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
 int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st);
 int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st);
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
+int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
+                  const void* x, void* y, cudaStream_t st);
+int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,
+                         int m, double* coef, int use_graph, cudaStream_t st);
+int project_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef, double* scratch,
+                   int64_t scratch_len, cudaStream_t st);
 int cf_launch(const double* a, const double* b, int m, const double* omega, int W, double e0, double eta,
               double norm2, double* out, cudaStream_t st);
 

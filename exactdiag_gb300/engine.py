@@ -160,9 +160,67 @@ class DeviceSector:
         nat.check("ed_accumulate",
                   self._lib.ed_accumulate(self._h, code, _ptr(x), c.real, c.imag, _ptr(acc), _stream_ptr()))
 
+    def project_out(self, basis: torch.Tensor, k: int, w: torch.Tensor, coef_out: torch.Tensor | None = None) -> None:
+        """w <- w - sum_{j<k} <basis[j], w> basis[j] (ed_project_out); coef_out float64 (2k,) gets the dots."""
+        code = self._code(w)
+        if basis.dtype != w.dtype or not basis.is_contiguous() or basis.shape[-1] != self.n or basis.shape[0] < k:
+            raise ValueError("basis must be a contiguous (>=k, n) tensor of the vector dtype")
+        if coef_out is not None and (coef_out.dtype != torch.float64 or coef_out.numel() < 2 * k):
+            raise ValueError("coef_out must be float64 with 2k entries")
+        nat.check("ed_project_out", self._lib.ed_project_out(self._h, code, _ptr(basis), int(k), _ptr(w),
+                                                             _ptr(coef_out), _stream_ptr()))
+
+    def excite_into(self, dst: "DeviceSector", name: str, qx: int, qy: int, initial_sz2: int, x: torch.Tensor,
+                    out: torch.Tensor | None = None) -> torch.Tensor:
+        """y = O x into sector dst (ed_excitation_apply); x, y complex."""
+        op = {"Szq": 0, "spectral_function_minus": 1}[str(name)]
+        if x.dtype not in (torch.complex128, torch.complex64) or x.numel() != self.n or not x.is_cuda:
+            raise ValueError("x must be a complex CUDA tensor of the source sector's length")
+        code = _CODE_OF_TORCH[x.dtype]
+        y = torch.empty(dst.n, dtype=x.dtype, device=dst.device) if out is None else out
+        nat.check("ed_excitation_apply",
+                  self._lib.ed_excitation_apply(self._h, dst._h, op, int(qx), int(qy), int(initial_sz2), code,
+                                                _ptr(x), _ptr(y), _stream_ptr()))
+        return y
+
     def normalize(self, x: torch.Tensor, norm_out: torch.Tensor) -> None:
         code = self._code(x)
         nat.check("ed_normalize", self._lib.ed_normalize(self._h, code, _ptr(x), _ptr(norm_out), _stream_ptr()))
+
+
+def batch_lanczos(sectors: list, weights, v0s: list, num_lanczos_vecs: int, use_graph: bool = True):
+    """Spectrum recursions of several sectors at once (ed_batch_lanczos).
+
+    Returns one (a, b, |v0|) per sector, truncated like _lanczos_get_anbn.
+    """
+    lib = nat.load()
+    m = int(num_lanczos_vecs)
+    nsec = len(sectors)
+    stride = 2 * m + 4
+    dev = sectors[0].device
+    coef = torch.zeros(nsec * stride, dtype=torch.float64, device=dev)
+    code = _CODE_OF_TORCH[v0s[0].dtype]
+    for s, v in zip(sectors, v0s):
+        s._code(v)
+        if v.dtype != v0s[0].dtype:
+            raise TypeError("all start vectors must share a dtype")
+    harr = (ctypes.c_void_p * nsec)(*[s._h.value for s in sectors])
+    varr = (ctypes.c_void_p * nsec)(*[v.data_ptr() for v in v0s])
+    w = nat.weights_array(weights_tuple(weights))
+    nat.check("ed_batch_lanczos", lib.ed_batch_lanczos(harr, nsec, w, code, varr, m, _ptr(coef), int(bool(use_graph)),
+                                                       _stream_ptr()))
+    x = coef.view(nsec, stride).cpu().numpy()
+    out = []
+    for s in range(nsec):
+        a = x[s, 1: 2 * m: 2].copy()
+        b_next = x[s, 2: 2 * m + 1: 2].copy()
+        k = m
+        small = np.nonzero(b_next < 1e-8)[0]
+        if len(small):
+            k = int(small[0]) + 1
+        b = np.concatenate([[0.0], b_next[: k - 1]])
+        out.append((a[:k], b[:k], float(x[s, stride - 1])))
+    return out
 
 
 def continued_fraction(a: torch.Tensor, b: torch.Tensor, omegas: torch.Tensor, e0: float, eta: float,

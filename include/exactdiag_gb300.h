@@ -109,6 +109,39 @@ int ed_normalize(const ed_sector* s, int dtype, void* x_dev, double* norm_dev, v
 int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const double* omega_dev, int W, double e0,
                           double eta, double norm2, double* out_dev, void* stream);
 
+/* Applies an excitation operator from sector src (initial, e.g. the ground
+ * state's) into sector dst: y = O x, pull-style over the rows of dst.
+ *   op 0: Szq = sum_r (1/2sqrt(N)) e^{-iq.r} S^z_r
+ *         (tJ_spin_half_ladder/matrix_setup.pyx:235-246; dst has the same Nh, Nd)
+ *   op 1: spectral_function_minus = sum_r (1/sqrt(N)) e^{-iq.r} c_{r,sigma},
+ *         sigma = down if initial_sz2 <= 0 else up (matrix_setup.pyx:302-325;
+ *         dst has Nh+1 holes and the removed spin)
+ * (qx, qy) are the operator quantum numbers as the matrix setup receives them;
+ * dst must be the sector the reference's target rule gives (matrix_setup.pyx:329-330).
+ * Vectors are complex: dtype ED_C128 or ED_C64, x of length n(src), y of n(dst).
+ * Replaces setup_excitation_operator's stored matrix and its .dot. */
+int ed_excitation_apply(const ed_sector* src, const ed_sector* dst, int op, int qx, int qy, int initial_sz2, int dtype,
+                        const void* x_src_dev, void* y_dst_dev, void* stream);
+
+/* Runs the spectrum Lanczos recursion (general/cython_lanczos_diagonalization.pyx:50-77)
+ * for nsec sectors together: m steps each from the start vectors v0_dev[s]
+ * (device pointers, dtype, any norm), all sectors' rows handled by one launch per
+ * phase and the m steps captured in one CUDA graph (use_graph != 0).  The
+ * sectors must share L, Nh and Nd.  coef_dev holds nsec * (2m+4) doubles
+ * (device); sector s's block X: X[2k+1] = a_k, X[2k+2] = b_{k+1}, X[2m+3] = |v0|.
+ * The caller truncates after the first b_{k+1} < 1e-8.  Synchronises `stream`.
+ * Replaces the per-q loop of tJ_spin_half_ladder/api.py:116-161 over
+ * general/lanczos_diagonalization.py:124-175. */
+int ed_batch_lanczos(const ed_sector* const* sectors, int nsec, const double weights[4], int dtype,
+                     const void* const* v0_dev, int m, double* coef_dev, int use_graph, void* stream);
+
+/* w <- w - sum_{j<k} <v_j, w> v_j for k vectors stored contiguously in basis_dev
+ * (k x n, dtype), dot products in FP64 (classical Gram-Schmidt; call twice for
+ * full reorthogonalisation).  coef_dev (device, 2k doubles, may be NULL)
+ * receives the coefficients <v_j, w> as (re, im) pairs.  The first call with a
+ * larger k grows a per-sector scratch buffer (a device allocation). */
+int ed_project_out(ed_sector* s, int dtype, const void* basis_dev, int k, void* w_dev, double* coef_dev, void* stream);
+
 /* Thread-local description of the last error. */
 const char* ed_last_error_string(void);
 

@@ -1,0 +1,228 @@
+"""GPU: excitation operators, eigen-solver, spectra and the drop-in API against the oracle and fixtures."""
+
+import numpy as np
+import pytest
+
+from conftest import fixture_sector, seeded_vector
+
+pytestmark = pytest.mark.gpu
+
+W = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
+NAMES = {0: "Szq", 1: "spectral_function_minus"}
+
+
+@pytest.fixture(scope="module")
+def torch(cuda):
+    return cuda
+
+
+@pytest.fixture()
+def in_tmp(tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    from exactdiag_gb300.tJ_spin_half_ladder import matrix_setup
+
+    yield tmp_path
+    matrix_setup.clear_sector_cache()
+
+
+def _sector(key):
+    from exactdiag_gb300.engine import DeviceSector
+
+    return DeviceSector(*key)
+
+
+def _cplx(torch, x, dev):
+    return torch.as_tensor(np.asarray(x, np.complex128), device=dev)
+
+
+EXC = [((6, 2, 5, 0, 0), "Szq", 1, 0), ((6, 2, 5, 0, 0), "Szq", 3, 1), ((5, 2, 4, 1, 0), "Szq", 2, 1),
+       ((6, 2, 5, 2, 1), "Szq", -1, 1), ((7, 1, 6, 3, 0), "Szq", 2, 0),
+       ((6, 0, 6, 0, 0), "spectral_function_minus", -1, 0), ((6, 0, 6, 0, 0), "spectral_function_minus", -2, 1),
+       ((5, 1, 4, 0, 1), "spectral_function_minus", -3, 0), ((6, 0, 6, 2, 1), "spectral_function_minus", 1, 1),
+       ((5, 2, 3, 1, 0), "spectral_function_minus", -1, 1), ((6, 1, 4, 0, 0), "spectral_function_minus", 2, 0)]
+
+
+@pytest.mark.parametrize("case", EXC)
+def test_excitation_vs_oracle(torch, oracle, case):
+    key, name, qx, qy = case
+    osec = oracle.Sector(*key)
+    ofsec = oracle.target_sector(osec, name, qx, qy)
+    bas, fbas = oracle.basis(osec), oracle.basis(ofsec)
+    m = oracle.excitation_matrix(osec, bas, name, qx, qy, ofsec, fbas)
+    x = seeded_vector(len(bas[0]), 17, True)
+    src, dst = _sector(key), _sector(ofsec.args())
+    y = src.excite_into(dst, name, qx, qy, osec.Sz2, _cplx(torch, x, src.device)).cpu().numpy()
+    assert np.max(np.abs(y - m @ x), initial=0) < 1e-12
+
+
+def test_excitation_vs_golden(torch, golden_excitations):
+    for idx, case in enumerate(golden_excitations["cases"]):
+        L, Nh, Nd, kx, ky, op, qx, qy = (int(v) for v in case)
+        src = _sector((L, Nh, Nd, kx, ky))
+        dst = _sector(tuple(int(v) for v in golden_excitations[f"e{idx}_target"]))
+        x = seeded_vector(src.n, int(golden_excitations[f"e{idx}_seed"][0]), True)
+        sz2 = 2 * L - Nh - 2 * Nd
+        y = src.excite_into(dst, NAMES[op], qx, qy, sz2, _cplx(torch, x, src.device)).cpu().numpy()
+        assert np.max(np.abs(y - golden_excitations[f"e{idx}_y"])) < 1e-12
+
+
+def test_eigenvalues_match_reference_fixtures(torch, reference_fixtures, in_tmp):
+    from exactdiag_gb300.eigensolver import lowest_eigenpairs
+    from exactdiag_gb300.engine import weights_tuple
+
+    checked = 0
+    for d in reference_fixtures:
+        if d.get("eigvals") is None:
+            continue
+        sec = _sector(fixture_sector(d))
+        vals, vecs = lowest_eigenpairs(sec, weights_tuple(d["weights"]), len(d["eigvals"]))
+        assert np.all(np.abs(vals - np.array(d["eigvals"])) < 1e-8), (d["file"], vals, d["eigvals"])
+        checked += 1
+    assert checked == 51
+
+
+@pytest.mark.parametrize("key", [(8, 2, 7, 0, 0), (7, 2, 6, 2, 1), (6, 0, 6, 0, 0)])
+def test_eigenpairs_vs_oracle(torch, oracle, key):
+    from exactdiag_gb300.eigensolver import lowest_eigenpairs
+
+    osec = oracle.Sector(*key)
+    h = oracle.hamiltonian(osec, W, oracle.basis(osec))
+    ref = oracle.lowest_eigvals(h, 5)
+    vals, vecs = lowest_eigenpairs(_sector(key), W, 5)
+    assert np.max(np.abs(vals - ref)) < 1e-9
+    for i in range(5):
+        v = vecs[:, i]
+        assert abs(np.linalg.norm(v) - 1) < 1e-9
+        assert np.linalg.norm(h @ v - vals[i] * v) < 1e-6
+
+
+def test_config1_lowest_four(torch):
+    # 2x8 ladder, 2 holes, k=(0,0): known answer of the reference's own stored H (FP64 eigsh, tol 1e-14)
+    from exactdiag_gb300.eigensolver import lowest_eigenpairs
+
+    vals, _ = lowest_eigenpairs(_sector((8, 2, 7, 0, 0)), W, 4)
+    assert np.max(np.abs(vals - np.array([-10.12086831, -9.85429876, -9.70467762, -9.63624331]))) < 6e-9
+
+
+def test_drop_in_hamiltonian_dot_and_translators(torch, oracle, in_tmp):
+    from exactdiag_gb300.tJ_spin_half_ladder import configs
+
+    cfg = configs.Hamiltonian_Config(num_rungs=6, num_holes=2, weights=W, symmetry_qs={"leg": 1, "rung": 1},
+                                     num_threads=4)
+    ham = cfg.setup()()
+    osec = oracle.Sector(6, 2, cfg.num_down_spins, 1, 1)
+    bas = oracle.basis(osec)
+    assert ham.shape == [len(bas[0])] * 2
+    x = seeded_vector(len(bas[0]), 4, True)
+    assert np.max(np.abs(ham.dot(x) - oracle.hamiltonian(osec, W, bas) @ x)) < 1e-12
+    trans, bmap, sym = cfg.get_translators()
+    assert bmap.get_num_states() == len(bas[0])
+    for i in (0, 7, len(bas[0]) - 1):
+        sp = bmap.get_sparse(i)
+        assert sp == bas[0][i] and bmap.get_dense(sp) == i
+        assert np.array_equal(trans.sparse_index_to_state(sp), oracle.sparse_to_state(osec, sp))
+        assert trans.state_to_sparse_index(trans.sparse_index_to_state(sp)) == sp
+    assert bmap.get_dense(-1) == -1 and sym.get_basis_length() == 12
+
+
+def test_lanczos_dynamical_response_vs_oracle(torch, oracle, in_tmp):
+    from exactdiag_gb300.general.lanczos_diagonalization import lanczos_dynamical_response
+    from exactdiag_gb300.general.sparse_matrices import Device_Hamiltonian, Device_Operator
+
+    key, name, qx, qy = (6, 2, 5, 0, 0), "Szq", 2, 1
+    osec = oracle.Sector(*key)
+    ofsec = oracle.target_sector(osec, name, qx, qy)
+    bas, fbas = oracle.basis(osec), oracle.basis(ofsec)
+    h0 = oracle.hamiltonian(osec, W, bas)
+    hf = oracle.hamiltonian(ofsec, W, fbas)
+    op = oracle.excitation_matrix(osec, bas, name, qx, qy, ofsec, fbas)
+    e, v = oracle.lowest_eigpairs(h0, 1)
+    zs = np.linspace(0, 6, 400) + e[0] + 0.05j
+    ref, ra, rb, _ = oracle.lanczos_dynamical_response(v[:, 0], lambda x: op @ x, lambda x: hf @ x, zs, 40)
+    src, dst = _sector(key), _sector(ofsec.args())
+    got = lanczos_dynamical_response(v[:, 0], Device_Operator(name, src, dst, qx, qy, osec.Sz2),
+                                     Device_Hamiltonian(dst, W), zs, 40)
+    assert np.max(np.abs(got - ref)) < 1e-8 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_batch_lanczos_matches_single(torch):
+    from exactdiag_gb300.engine import batch_lanczos
+    from exactdiag_gb300.lanczos import lanczos_coefficients
+
+    secs = [_sector((6, 2, 5, kx, ky)) for kx in range(3) for ky in range(2)]
+    v0s = [torch.as_tensor(seeded_vector(s.n, 30 + i, True), device=s.device) for i, s in enumerate(secs)]
+    for graph in (True, False):
+        outs = batch_lanczos(secs, W, v0s, 25, use_graph=graph)
+        for s, v, (a, b, nrm) in zip(secs, v0s, outs):
+            a1, b1, n1 = lanczos_coefficients(s, W, v.clone(), 25)
+            k = min(len(a), len(a1), 12)
+            assert np.max(np.abs(a[:k] - a1[:k])) < 1e-10 and np.max(np.abs(b[:k] - b1[:k])) < 1e-10
+            assert abs(nrm - n1) < 1e-10
+
+
+def _spectrum_config(L, Nh, name, broadening=0.05, omega_min=0.0, omega_max=6.0, steps=300, m=60):
+    from exactdiag_gb300.tJ_spin_half_ladder import configs
+
+    return configs.Full_Spectrum_Config(
+        hamiltonian={"num_rungs": L, "num_holes": Nh, "weights": W, "symmetry_qs": {"leg": 0, "rung": 0},
+                     "num_threads": 1},
+        eigenpair={"num_eigenpairs": 3},
+        spectrum={"name": name, "operator_symmetry_qs": {"leg": 0, "rung": 0}, "broadening": broadening,
+                  "omega_min": omega_min, "omega_max": omega_max, "omega_steps": steps, "num_lanczos_vecs": m})
+
+
+def test_szq_spectra_batched_equals_sequential(torch, in_tmp):
+    import shutil
+
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+
+    cfg = _spectrum_config(6, 2, "Szq")
+    ws_b, sp_b, _ = api.get_Szq_spectra(cfg, limited_qs=False, batched=True)
+    shutil.rmtree(in_tmp / "calculations")
+    ws_s, sp_s, _ = api.get_Szq_spectra(cfg, limited_qs=False, batched=False)
+    assert sp_b.shape == (6, 2, 300)
+    assert np.max(np.abs(sp_b - sp_s)) < 1e-6
+    assert np.all(np.isfinite(sp_b)) and np.max(sp_b) > 0
+
+
+def test_spectral_function_minus_batched_equals_sequential(torch, in_tmp):
+    import shutil
+
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+
+    cfg = _spectrum_config(6, 0, "spectral_function_minus", omega_min=-4, omega_max=8)
+    ws_b, sp_b, info = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=True)
+    shutil.rmtree(in_tmp / "calculations")
+    ws_s, sp_s, _ = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=False)
+    assert sp_b.shape[0] == 1
+    assert np.max(np.abs(sp_b - sp_s)) < 1e-6
+
+
+def test_spectrum_vs_oracle_pipeline(torch, oracle, in_tmp):
+    """One Szq spectrum end to end against the oracle restatement of the reference pipeline."""
+    from exactdiag_gb300.general import lanczos_diagonalization as ld
+
+    cfg = _spectrum_config(5, 2, "Szq", m=40)
+    cfg.spectrum.operator_symmetry_qs = {"leg": 2, "rung": 1}
+    ws, got = ld.get_spectrum(cfg)
+    key = (5, 2, cfg.hamiltonian.num_down_spins, 0, 0)
+    osec = oracle.Sector(*key)
+    ofsec = oracle.target_sector(osec, "Szq", 2, 1)
+    bas, fbas = oracle.basis(osec), oracle.basis(ofsec)
+    h0 = oracle.hamiltonian(osec, W, bas)
+    e, v = oracle.lowest_eigpairs(h0, 3)
+    op = oracle.excitation_matrix(osec, bas, "Szq", 2, 1, ofsec, fbas)
+    hf = oracle.hamiltonian(ofsec, W, fbas)
+    zs = ws + e[0] + 0.05j
+    ref = np.zeros(len(ws))
+    nd = 0
+    for j in range(3):
+        if abs(e[0] - e[j]) > 1e-6:
+            break
+        nd += 1
+        ref += oracle.lanczos_dynamical_response(v[:, j], lambda x: op @ x, lambda x: hf @ x, zs, 40)[0]
+    ref /= nd
+    if nd == 1:
+        assert np.max(np.abs(got - ref)) < 1e-7 * max(1.0, np.max(np.abs(ref)))
+    else:  # a degenerate ground state: the average does not depend on the basis of the eigenspace
+        assert np.max(np.abs(got - ref)) < 1e-5 * max(1.0, np.max(np.abs(ref)))

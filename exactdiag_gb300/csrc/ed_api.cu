@@ -138,9 +138,7 @@ int ed_basis_build(ed_sector* h, void* stream) {
     if (per_sm <= 0) per_sm = 1;
     if (per_sm > 8) per_sm = 8;
     s.hv_grid = s.num_sms * per_sm;
-    if (!s.d_partials.alloc((int64_t)s.hv_grid * kReduceSlots))
-        return set_error(ED_ERR_NOMEM, "ed_basis_build: reduction scratch");
-    return ED_OK;
+    return single_setup(s);
 }
 
 int ed_basis_size(const ed_sector* h, int64_t* n) {

@@ -18,12 +18,6 @@
 
 namespace ed {
 
-struct BatchChunk {
-    int32_t sec;
-    int32_t pad;
-    int64_t begin, end;  // rows of sector `sec`
-};
-
 constexpr int kChunkRows = 1 << 16;
 
 __device__ __forceinline__ void chunk_reduce(double v[kReduceSlots], double* __restrict__ out) {
@@ -56,9 +50,9 @@ __device__ __forceinline__ void* vec_at(void* base, int64_t off) {
 
 template <typename R, bool CPLX>
 __global__ void __launch_bounds__(kHvThreads)
-    batch_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
-                    const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* other, int first,
-                    const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
+    lanczos_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
+                    const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* vprev, void* other,
+                    int first, const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
     extern __shared__ __align__(16) uint8_t smem[];
     const HvTables<R> tb = load_tables<R>(views[0], smem);
     const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
@@ -67,6 +61,7 @@ __global__ void __launch_bounds__(kHvThreads)
         const SectorView S = views[ch.sec];
         const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
         void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
+        const void* yp = first ? nullptr : vec_at<R, CPLX>(vprev, offs[ch.sec]);
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
         double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
         for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
@@ -75,7 +70,7 @@ __global__ void __launch_bounds__(kHvThreads)
             R yr = hr, yi = hi;
             if (!first) {
                 R pr, pi;
-                ld<R, CPLX>(y, i, pr, pi);  // y holds v_{k-1} before it is overwritten by this row
+                ld<R, CPLX>(yp, i, pr, pi);  // v_{k-1}; may be the same buffer as y (read before written)
                 yr -= beta * pr;
                 yi -= beta * pi;
             }
@@ -91,9 +86,9 @@ __global__ void __launch_bounds__(kHvThreads)
 }
 
 // One CTA per sector: a_k, b_{k+1} from the sector's chunk partials (fixed order).
-__global__ void batch_scalars_kernel(const double* __restrict__ partials, const int* __restrict__ cfirst,
-                                     const int* __restrict__ ccount, double* __restrict__ scal, int stride, int k,
-                                     int norm_mode) {
+__global__ void lanczos_scalars_kernel(const double* __restrict__ partials, const int* __restrict__ cfirst,
+                                      const int* __restrict__ ccount, double* __restrict__ scal, int stride, int k,
+                                      int norm_mode, int norm_off) {
     __shared__ double red[kReduceSlots][32];
     const int s = blockIdx.x;
     double t[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
@@ -117,7 +112,7 @@ __global__ void batch_scalars_kernel(const double* __restrict__ partials, const 
         }
         double* X = scal + (int64_t)s * stride;
         if (norm_mode) {
-            X[stride - 1] = sqrt(tot[3]);  // |v0|
+            X[norm_off] = sqrt(tot[3]);  // |v0|
             return;
         }
         const double a = tot[0];
@@ -130,7 +125,7 @@ __global__ void batch_scalars_kernel(const double* __restrict__ partials, const 
 }
 
 template <typename R, bool CPLX>
-__global__ void batch_norm_partials_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+__global__ void norm_partials_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
                                            int nchunks, const void* v, double* __restrict__ partials) {
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
@@ -147,15 +142,15 @@ __global__ void batch_norm_partials_kernel(const int64_t* __restrict__ offs, con
 
 // mode 0: v_next = (y - a v) / b (step update); mode 1: v *= 1/|v0| (start vector)
 template <typename R, bool CPLX>
-__global__ void batch_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
-                                    int nchunks, void* v, void* other, const double* __restrict__ scal, int stride,
-                                    int k, int mode) {
+__global__ void lanczos_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+                                     int nchunks, void* v, void* other, const double* __restrict__ scal, int stride,
+                                     int k, int mode, int norm_off) {
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
         const double* X = scal + (int64_t)ch.sec * stride;
         void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
         if (mode == 1) {
-            const double nv = X[stride - 1];
+            const double nv = X[norm_off];
             const R inv = nv > 0.0 ? (R)(1.0 / nv) : R(0);
             for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
                 R xr, xi;
@@ -177,6 +172,17 @@ __global__ void batch_update_kernel(const int64_t* __restrict__ offs, const Batc
     }
 }
 
+// Chunk table of one sector (rows [0, n) cut every kChunkRows), appended to `out`.
+static void append_chunks(int sec, int64_t n, std::vector<BatchChunk>& out) {
+    for (int64_t b = 0; b < n; b += kChunkRows) {
+        BatchChunk c{};
+        c.sec = sec;
+        c.begin = b;
+        c.end = std::min<int64_t>(n, b + kChunkRows);
+        out.push_back(c);
+    }
+}
+
 template <typename R, bool CPLX>
 static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& w, const void* const* v0, int m,
                        double* coef, int use_graph, cudaStream_t st) {
@@ -191,13 +197,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         hviews[s] = secs[s]->view;
         hoffs[s] = total;
         cfirst[s] = (int)hchunks.size();
-        for (int64_t b = 0; b < hviews[s].n; b += kChunkRows) {
-            BatchChunk c{};
-            c.sec = s;
-            c.begin = b;
-            c.end = std::min<int64_t>(hviews[s].n, b + kChunkRows);
-            hchunks.push_back(c);
-        }
+        append_chunks(s, hviews[s].n, hchunks);
         ccount[s] = (int)hchunks.size() - cfirst[s];
         total += hviews[s].n;
     }
@@ -223,12 +223,12 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
             cudaMemcpyAsync(buf0.p + hoffs[s] * esz, v0[s], hviews[s].n * esz, cudaMemcpyDeviceToDevice, st);
     const int grid = std::min(nchunks, secs[0]->hv_grid > 0 ? secs[0]->hv_grid : secs[0]->num_sms * 3);
     const size_t smem = hv_smem_bytes(hviews[0], sizeof(R));
-    cudaFuncSetAttribute(batch_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // start vectors: |v0| and normalisation
-    batch_norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
-    batch_scalars_kernel<<<nsec, 256, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1);
-    batch_update_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
-                                                       1);
+    norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
+    lanczos_scalars_kernel<<<nsec, 256, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1, stride - 1);
+    lanczos_update_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
+                                                        1, stride - 1);
     ED_CHECK_LAUNCH("batch start vectors");
     cudaStream_t cap = st;
     cudaStream_t priv = nullptr;
@@ -245,10 +245,11 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     for (int k = 0; k < m; ++k) {
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
-        batch_hv_kernel<R, CPLX><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
-                                                                  k == 0, coef, stride, k, partials.p);
-        batch_scalars_kernel<<<nsec, 256, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0);
-        batch_update_kernel<R, CPLX><<<grid, 256, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0);
+        lanczos_hv_kernel<R, CPLX><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
+                                                                    other, k == 0, coef, stride, k, partials.p);
+        lanczos_scalars_kernel<<<nsec, 256, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
+        lanczos_update_kernel<R, CPLX><<<grid, 256, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0,
+                                                             0);
     }
     if (use_graph) {
         cudaGraph_t graph = nullptr;
@@ -286,6 +287,112 @@ int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights
     case ED_C64: return batch_typed<float, true>(secs, w, v0, m, coef, use_graph, st);
     default: return set_error(ED_ERR_INVALID, "ed_batch_lanczos: dtype");
     }
+}
+
+// ------------------------------------------------------------ single sector
+//
+// A single sector runs through the same kernels as a batch of one (same chunks,
+// same reduction order), so sequential and batched recursions agree bit for bit.
+
+int single_setup(Sector& s) {
+    std::vector<BatchChunk> ch;
+    append_chunks(0, s.view.n, ch);
+    const int64_t zero = 0;
+    const int first = 0, count = (int)ch.size();
+    s.n_chunks = count;
+    if (!s.d_self.alloc(1) || !s.d_offs.alloc(1) || !s.d_chunks.alloc(count > 0 ? count : 1) ||
+        !s.d_cfirst.alloc(1) || !s.d_ccount.alloc(1))
+        return set_error(ED_ERR_NOMEM, "sector step tables");
+    cudaMemcpy(s.d_self.p, &s.view, sizeof(SectorView), cudaMemcpyHostToDevice);
+    cudaMemcpy(s.d_offs.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (count) cudaMemcpy(s.d_chunks.p, ch.data(), count * sizeof(BatchChunk), cudaMemcpyHostToDevice);
+    cudaMemcpy(s.d_cfirst.p, &first, sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(s.d_ccount.p, &count, sizeof(int), cudaMemcpyHostToDevice);
+    const int64_t slots = (int64_t)std::max(count, s.hv_grid) * kReduceSlots;
+    if (!s.d_partials.alloc(slots)) return set_error(ED_ERR_NOMEM, "sector reduction scratch");
+    return ED_OK;
+}
+
+static bool dtype_fits(const Sector& s, int dtype) {
+    if (dtype == ED_C128 || dtype == ED_C64) return true;
+    if (dtype == ED_F64 || dtype == ED_F32) return s.real;
+    return false;
+}
+
+static int step_grid(const Sector& s) { return std::max(1, std::min(s.n_chunks, s.hv_grid)); }
+
+template <typename R, bool CPLX>
+static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
+                           double* scal, cudaStream_t st) {
+    const size_t smem = hv_smem_bytes(s.view, sizeof(R));
+    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lanczos_hv_kernel<R, CPLX><<<step_grid(s), kHvThreads, smem, st>>>(
+        s.d_self.p, s.d_offs.p, s.d_chunks.p, s.n_chunks, w, const_cast<void*>(v), const_cast<void*>(vprev), vnext,
+        vprev == nullptr, scal, 0, 0, s.d_partials.p);
+    ED_CHECK_LAUNCH("lanczos_hv_kernel");
+    lanczos_scalars_kernel<<<1, 256, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
+    ED_CHECK_LAUNCH("lanczos_scalars_kernel");
+    return ED_OK;
+}
+
+int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
+                      double* scal, double* /*partials*/, cudaStream_t st) {
+    if (!dtype_fits(s, dtype)) return set_error(ED_ERR_INVALID, "ed_lanczos_step: dtype does not match the sector");
+    if (s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_lanczos_step: empty sector");
+    switch (dtype) {
+    case ED_F64: return single_hv_typed<double, false>(s, w, v, vprev, vnext, scal, st);
+    case ED_C128: return single_hv_typed<double, true>(s, w, v, vprev, vnext, scal, st);
+    case ED_F32: return single_hv_typed<float, false>(s, w, v, vprev, vnext, scal, st);
+    default: return single_hv_typed<float, true>(s, w, v, vprev, vnext, scal, st);
+    }
+}
+
+template <typename R, bool CPLX>
+static void single_update_typed(const Sector& s, const void* v, void* vnext, const double* scal, cudaStream_t st) {
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks,
+                                                                 const_cast<void*>(v), vnext, scal, 0, 0, 0, 0);
+}
+
+int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st) {
+    if (!dtype_fits(s, dtype)) return set_error(ED_ERR_INVALID, "ed_lanczos_update: dtype does not match the sector");
+    if (s.view.n == 0) return ED_OK;
+    switch (dtype) {
+    case ED_F64: single_update_typed<double, false>(s, v, vnext, scal, st); break;
+    case ED_C128: single_update_typed<double, true>(s, v, vnext, scal, st); break;
+    case ED_F32: single_update_typed<float, false>(s, v, vnext, scal, st); break;
+    default: single_update_typed<float, true>(s, v, vnext, scal, st); break;
+    }
+    ED_CHECK_LAUNCH("lanczos_update_kernel");
+    return ED_OK;
+}
+
+int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,
+                        double* scal, double* partials, cudaStream_t st) {
+    const int rc = lanczos_hv_launch(s, w, dtype, v, vprev, vnext, scal, partials, st);
+    if (rc != ED_OK) return rc;
+    return lanczos_update_launch(s, dtype, v, vnext, scal, st);
+}
+
+template <typename R, bool CPLX>
+static void single_norm_typed(const Sector& s, void* x, double* norm, cudaStream_t st) {
+    norm_partials_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x,
+                                                                s.d_partials.p);
+    lanczos_scalars_kernel<<<1, 256, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, norm, 0, 0, 1, 0);
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x, nullptr,
+                                                                 norm, 0, 0, 1, 0);
+}
+
+int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* /*partials*/, cudaStream_t st) {
+    if (!dtype_fits(s, dtype)) return set_error(ED_ERR_INVALID, "ed_normalize: dtype does not match the sector");
+    if (s.view.n == 0) return ED_OK;
+    switch (dtype) {
+    case ED_F64: single_norm_typed<double, false>(s, x, norm, st); break;
+    case ED_C128: single_norm_typed<double, true>(s, x, norm, st); break;
+    case ED_F32: single_norm_typed<float, false>(s, x, norm, st); break;
+    default: single_norm_typed<float, true>(s, x, norm, st); break;
+    }
+    ED_CHECK_LAUNCH("normalize kernels");
+    return ED_OK;
 }
 
 // ------------------------------------------------------------ projection

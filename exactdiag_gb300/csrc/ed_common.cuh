@@ -155,6 +155,7 @@ struct OrbitResult {
     int found;      // orbit size as the reference counts it, 0 = not lowest / incompatible
     uint64_t low;   // lowest image (first strictly-lowest in the reference's list order)
     int e;          // phase exponent of the lowest image, mod 2L
+    int p;          // product index of the lowest image (0 = the state itself)
 };
 
 // Restatement of Symmetries_Single_Spin_Half_2leg_Ladder::get_symmetry_states_from_state
@@ -171,7 +172,7 @@ __host__ __device__ __forceinline__ OrbitResult orbit_walk(int L, int kx, int ky
     const int P = L - popc32(any_hole);
     const int e_mirror = (L * ky + L * (P & 1)) % twoL;
     const uint32_t hm = mirror_legs(h), dm = mirror_legs(d);
-    int eT = 0, found = 1, e1 = 0, elow = 0;
+    int eT = 0, found = 1, e1 = 0, elow = 0, plow = 0;
     bool msym = false;
     uint64_t img1 = 0, low = key;
     for (int p = 1; p < N; ++p) {
@@ -190,10 +191,10 @@ __host__ __device__ __forceinline__ OrbitResult orbit_walk(int L, int kx, int ky
             eT %= twoL;
             e = eT;
         }
-        if (check_lowest && img < key) return {0, 0, 0};
+        if (check_lowest && img < key) return {0, 0, 0, 0};
         if (s < L / 2 + 1) {
             if (img == key) {
-                if (e != 0) return {0, 0, 0};
+                if (e != 0) return {0, 0, 0, 0};
                 if (p == 1) {
                     msym = true;
                     continue;
@@ -201,7 +202,7 @@ __host__ __device__ __forceinline__ OrbitResult orbit_walk(int L, int kx, int ky
                 break;
             }
             if (found != 1 && img == img1) {
-                if (e != e1) return {0, 0, 0};
+                if (e != e1) return {0, 0, 0, 0};
                 break;
             }
         }
@@ -213,9 +214,10 @@ __host__ __device__ __forceinline__ OrbitResult orbit_walk(int L, int kx, int ky
         if (img < low) {
             low = img;
             elow = e;
+            plow = p;
         }
     }
-    return {found, low, elow};
+    return {found, low, elow, plow};
 }
 
 }  // namespace ed

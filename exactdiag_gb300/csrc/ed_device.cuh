@@ -77,6 +77,7 @@ struct Resolved {
     int64_t j;  // dense row of the representative, -1 if absent or incompatible
     int nj;     // orbit size of the new state
     int e;      // phase exponent (units of pi/L) of its lowest image
+    int p;      // product index of the group element that gives the lowest image
 };
 
 // Representative of the configuration (h2, d2) in sector S: dense row, orbit
@@ -85,9 +86,9 @@ struct Resolved {
 __device__ __forceinline__ Resolved resolve(const SectorView& S, const uint32_t* rank_tab, const uint32_t* comb,
                                             uint32_t h2, uint32_t d2) {
     const HoleEntry he = S.holes[hole_rank(h2, comb)];
-    if (he.block < 0) return {-1, 0, 0};
+    if (he.block < 0) return {-1, 0, 0, 0};
     const BlockInfo B = S.blocks[he.block];
-    int nj, e;
+    int nj, e, p;
     uint32_t dr;
     if (he.free_) {
         uint32_t hh = h2;
@@ -95,14 +96,16 @@ __device__ __forceinline__ Resolved resolve(const SectorView& S, const uint32_t*
         apply_p(he.p_star, hh, dr, S.N, S.mask);
         nj = S.N;
         e = he.e_star;
+        p = he.p_star;
     } else {
         const OrbitResult o = orbit_walk(S.L, S.kx, S.ky, S.ne_even, S.mask, h2, d2, false);
-        if (o.found == 0) return {-1, 0, 0};
+        if (o.found == 0) return {-1, 0, 0, 0};
         dr = (uint32_t)o.low;
         nj = o.found;
         e = o.e;
+        p = o.p;
     }
-    return {dense_in_block(S, B, dr, rank_tab), nj, e};
+    return {dense_in_block(S, B, dr, rank_tab), nj, e, p};
 }
 
 // Accumulate conj(M[j,i]) x_j for the new state (h2, d2); `coef` already holds

@@ -25,6 +25,7 @@ namespace ed {
 struct ExciteParams {
     int op;
     int add_down;      // c_minus: the removed (pull: re-added) spin is down
+    int qx, qy;
     double wr[kMaxN];  // w_r
     double wi[kMaxN];
 };
@@ -73,10 +74,19 @@ __global__ void __launch_bounds__(kHvThreads)
                 if (rv.j < 0) continue;
                 const uint32_t above = (r == 31) ? 0u : (~0u << (r + 1));
                 const double sgn = (__popc(occ & above) & 1) ? -1.0 : 1.0;
+                // The reference evaluates this term from the source representative, at the site
+                // rs = g(r) where g maps the new configuration to its lowest image, with w_rs rounded
+                // in single precision; w_r = w_rs * exp(+i q.(rs - r)) exactly.
+                const int shift = rv.p >> 1, mir = rv.p & 1;
+                int rs = (mir ? (r ^ 1) : r) + 2 * shift;
+                if (rs >= N) rs -= N;
+                double sq, cq;
+                sincospi(2.0 * (double)P.qx * (double)shift / (double)S.L + (double)(P.qy * mir), &sq, &cq);
+                const double wr = P.wr[rs] * cq - P.wi[rs] * sq, wi = P.wr[rs] * sq + P.wi[rs] * cq;
                 double sp, cp;
                 sincospi((double)rv.e / (double)S.L, &sp, &cp);
                 const double f = sgn * sqNj / sqrt((double)rv.nj);
-                const double vr = f * (P.wr[r] * cp - P.wi[r] * sp), vi = f * (P.wr[r] * sp + P.wi[r] * cp);
+                const double vr = f * (wr * cp - wi * sp), vi = f * (wr * sp + wi * cp);
                 R xr, xi;
                 ld<R, true>(x, rv.j, xr, xi);
                 accr += vr * (double)xr - vi * (double)xi;
@@ -109,6 +119,8 @@ int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, 
         return set_error(ED_ERR_INVALID, "ed_excitation_apply: target sector momentum does not match k + q");
     ExciteParams P{};
     P.op = op;
+    P.qx = qx;
+    P.qy = qy;
     double base;
     if (op == 0) {
         if (T.Nh != S.Nh || T.Nd != S.Nd) return set_error(ED_ERR_INVALID, "ed_excitation_apply: Szq keeps Nh, Nd");

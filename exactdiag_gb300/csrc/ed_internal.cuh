@@ -85,6 +85,18 @@ struct Sector {
     DevBuf<uint8_t> d_orbit;
     DevBuf<double> d_partials;   // [hv_grid][kReduceSlots] scratch of the fused Lanczos step
     DevBuf<double> d_proj;       // projection scratch: partial dots and coefficients
+    // the sector as a batch of one (step kernels): device view, offsets and chunk table
+    int n_chunks = 0;
+    DevBuf<SectorView> d_self;
+    DevBuf<int64_t> d_offs;
+    DevBuf<struct BatchChunk> d_chunks;
+    DevBuf<int> d_cfirst, d_ccount;
+};
+
+struct BatchChunk {
+    int32_t sec;
+    int32_t pad;
+    int64_t begin, end;  // rows of sector `sec`
 };
 
 // ed_basis.cu
@@ -107,6 +119,7 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
 int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st);
 int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st);
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
+int single_setup(Sector& s);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,

@@ -42,6 +42,21 @@ EXC = [((6, 2, 5, 0, 0), "Szq", 1, 0), ((6, 2, 5, 0, 0), "Szq", 3, 1), ((5, 2, 4
        ((5, 2, 3, 1, 0), "spectral_function_minus", -1, 1), ((6, 1, 4, 0, 0), "spectral_function_minus", 2, 0)]
 
 
+def _excitation_tolerance(name, key, y_ref):
+    """Szq, and c_minus from free source hole patterns, match the reference to rounding.
+
+    For c_minus out of a stabilised source configuration (the undoped sectors) the reference
+    sums |Stab| column terms whose phases e^{-iq.r} it rounds in single precision
+    (general/group/symmetry_generator.h:87-102, int*int/float); the pull form here carries one
+    term per target hole, so the two roundings differ.  The reference's own phase error is
+    0.5-3e-7 relative on these cases (its float phases against exact ones); the bound below is
+    the same order.
+    """
+    if name == "spectral_function_minus" and key[1] == 0:
+        return 2e-7 * max(1.0, float(np.max(np.abs(y_ref), initial=0)))
+    return 1e-12
+
+
 @pytest.mark.parametrize("case", EXC)
 def test_excitation_vs_oracle(torch, oracle, case):
     key, name, qx, qy = case
@@ -52,7 +67,8 @@ def test_excitation_vs_oracle(torch, oracle, case):
     x = seeded_vector(len(bas[0]), 17, True)
     src, dst = _sector(key), _sector(ofsec.args())
     y = src.excite_into(dst, name, qx, qy, osec.Sz2, _cplx(torch, x, src.device)).cpu().numpy()
-    assert np.max(np.abs(y - m @ x), initial=0) < 1e-12
+    y_ref = m @ x
+    assert np.max(np.abs(y - y_ref), initial=0) < _excitation_tolerance(name, key, y_ref)
 
 
 def test_excitation_vs_golden(torch, golden_excitations):
@@ -63,7 +79,8 @@ def test_excitation_vs_golden(torch, golden_excitations):
         x = seeded_vector(src.n, int(golden_excitations[f"e{idx}_seed"][0]), True)
         sz2 = 2 * L - Nh - 2 * Nd
         y = src.excite_into(dst, NAMES[op], qx, qy, sz2, _cplx(torch, x, src.device)).cpu().numpy()
-        assert np.max(np.abs(y - golden_excitations[f"e{idx}_y"])) < 1e-12
+        y_ref = golden_excitations[f"e{idx}_y"]
+        assert np.max(np.abs(y - y_ref)) < _excitation_tolerance(NAMES[op], (L, Nh), y_ref)
 
 
 def test_eigenvalues_match_reference_fixtures(torch, reference_fixtures, in_tmp):
@@ -126,10 +143,15 @@ def test_drop_in_hamiltonian_dot_and_translators(torch, oracle, in_tmp):
 
 
 def test_lanczos_dynamical_response_vs_oracle(torch, oracle, in_tmp):
+    """phi = O|gs>, the recursion's coefficients and the continued fraction against the oracle.
+
+    The unreorthogonalised recursion amplifies rounding differences once Ritz values converge,
+    so the end-to-end comparison uses 12 steps (before convergence on this sector).
+    """
     from exactdiag_gb300.general.lanczos_diagonalization import lanczos_dynamical_response
     from exactdiag_gb300.general.sparse_matrices import Device_Hamiltonian, Device_Operator
 
-    key, name, qx, qy = (6, 2, 5, 0, 0), "Szq", 2, 1
+    key, name, qx, qy = (7, 2, 6, 0, 0), "Szq", 2, 1
     osec = oracle.Sector(*key)
     ofsec = oracle.target_sector(osec, name, qx, qy)
     bas, fbas = oracle.basis(osec), oracle.basis(ofsec)
@@ -138,11 +160,13 @@ def test_lanczos_dynamical_response_vs_oracle(torch, oracle, in_tmp):
     op = oracle.excitation_matrix(osec, bas, name, qx, qy, ofsec, fbas)
     e, v = oracle.lowest_eigpairs(h0, 1)
     zs = np.linspace(0, 6, 400) + e[0] + 0.05j
-    ref, ra, rb, _ = oracle.lanczos_dynamical_response(v[:, 0], lambda x: op @ x, lambda x: hf @ x, zs, 40)
+    ref, ra, rb, _ = oracle.lanczos_dynamical_response(v[:, 0], lambda x: op @ x, lambda x: hf @ x, zs, 12)
     src, dst = _sector(key), _sector(ofsec.args())
-    got = lanczos_dynamical_response(v[:, 0], Device_Operator(name, src, dst, qx, qy, osec.Sz2),
-                                     Device_Hamiltonian(dst, W), zs, 40)
-    assert np.max(np.abs(got - ref)) < 1e-8 * max(1.0, np.max(np.abs(ref)))
+    dop = Device_Operator(name, src, dst, qx, qy, osec.Sz2)
+    phi = dop.dot(v[:, 0])
+    assert np.max(np.abs(phi - op @ v[:, 0])) < 1e-12
+    got = lanczos_dynamical_response(v[:, 0], dop, Device_Hamiltonian(dst, W), zs, 12)
+    assert np.max(np.abs(got - ref)) < 1e-9 * max(1.0, np.max(np.abs(ref)))
 
 
 def test_batch_lanczos_matches_single(torch):
@@ -181,7 +205,8 @@ def test_szq_spectra_batched_equals_sequential(torch, in_tmp):
     shutil.rmtree(in_tmp / "calculations")
     ws_s, sp_s, _ = api.get_Szq_spectra(cfg, limited_qs=False, batched=False)
     assert sp_b.shape == (6, 2, 300)
-    assert np.max(np.abs(sp_b - sp_s)) < 1e-6
+    # same kernels, same chunking and reduction order: batched equals sequential bit for bit
+    assert np.max(np.abs(sp_b - sp_s)) == 0.0
     assert np.all(np.isfinite(sp_b)) and np.max(sp_b) > 0
 
 
@@ -195,34 +220,28 @@ def test_spectral_function_minus_batched_equals_sequential(torch, in_tmp):
     shutil.rmtree(in_tmp / "calculations")
     ws_s, sp_s, _ = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=False)
     assert sp_b.shape[0] == 1
-    assert np.max(np.abs(sp_b - sp_s)) < 1e-6
+    assert np.max(np.abs(sp_b - sp_s)) == 0.0
 
 
 def test_spectrum_vs_oracle_pipeline(torch, oracle, in_tmp):
-    """One Szq spectrum end to end against the oracle restatement of the reference pipeline."""
+    """One Szq spectrum through get_spectrum (eigenpairs, operator, recursion, continued fraction, cache file)."""
     from exactdiag_gb300.general import lanczos_diagonalization as ld
 
-    cfg = _spectrum_config(5, 2, "Szq", m=40)
+    cfg = _spectrum_config(7, 2, "Szq", m=12)
     cfg.spectrum.operator_symmetry_qs = {"leg": 2, "rung": 1}
     ws, got = ld.get_spectrum(cfg)
-    key = (5, 2, cfg.hamiltonian.num_down_spins, 0, 0)
+    assert cfg.get_spectrum_path("").is_file()
+    key = (7, 2, cfg.hamiltonian.num_down_spins, 0, 0)
     osec = oracle.Sector(*key)
     ofsec = oracle.target_sector(osec, "Szq", 2, 1)
     bas, fbas = oracle.basis(osec), oracle.basis(ofsec)
     h0 = oracle.hamiltonian(osec, W, bas)
     e, v = oracle.lowest_eigpairs(h0, 3)
+    assert abs(e[1] - e[0]) > 1e-6  # non-degenerate ground state: the spectrum is basis independent
     op = oracle.excitation_matrix(osec, bas, "Szq", 2, 1, ofsec, fbas)
     hf = oracle.hamiltonian(ofsec, W, fbas)
     zs = ws + e[0] + 0.05j
-    ref = np.zeros(len(ws))
-    nd = 0
-    for j in range(3):
-        if abs(e[0] - e[j]) > 1e-6:
-            break
-        nd += 1
-        ref += oracle.lanczos_dynamical_response(v[:, j], lambda x: op @ x, lambda x: hf @ x, zs, 40)[0]
-    ref /= nd
-    if nd == 1:
-        assert np.max(np.abs(got - ref)) < 1e-7 * max(1.0, np.max(np.abs(ref)))
-    else:  # a degenerate ground state: the average does not depend on the basis of the eigenspace
-        assert np.max(np.abs(got - ref)) < 1e-5 * max(1.0, np.max(np.abs(ref)))
+    ref = oracle.lanczos_dynamical_response(v[:, 0], lambda x: op @ x, lambda x: hf @ x, zs, 12)[0]
+    assert np.max(np.abs(got - ref)) < 1e-8 * max(1.0, np.max(np.abs(ref)))
+    ws2, again = ld.get_spectrum(cfg)  # second call loads the cached file
+    assert np.array_equal(again, got)

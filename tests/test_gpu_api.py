@@ -179,9 +179,8 @@ def test_batch_lanczos_matches_single(torch):
         outs = batch_lanczos(secs, W, v0s, 25, use_graph=graph)
         for s, v, (a, b, nrm) in zip(secs, v0s, outs):
             a1, b1, n1 = lanczos_coefficients(s, W, v.clone(), 25)
-            k = min(len(a), len(a1), 12)
-            assert np.max(np.abs(a[:k] - a1[:k])) < 1e-10 and np.max(np.abs(b[:k] - b1[:k])) < 1e-10
-            assert abs(nrm - n1) < 1e-10
+            # one kernel set, same chunking and reduction order: identical to the last bit
+            assert np.array_equal(a, a1) and np.array_equal(b, b1) and nrm == n1
 
 
 def _spectrum_config(L, Nh, name, broadening=0.05, omega_min=0.0, omega_max=6.0, steps=300, m=60):

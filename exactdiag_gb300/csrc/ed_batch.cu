@@ -18,7 +18,9 @@
 
 namespace ed {
 
-constexpr int kChunkRows = 1 << 16;
+// Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
+// (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
+constexpr int kChunkRows = 2048;
 
 __device__ __forceinline__ void chunk_reduce(double v[kReduceSlots], double* __restrict__ out) {
     __shared__ double red[kReduceSlots][32];

@@ -123,6 +123,20 @@ def ncu_traffic(workload_key: str) -> float | None:
     return float(fields["dram_bytes_per_launch"])
 
 
+def aggregate_replicas(ms_local: list[float], steps: int, world: int, device=None) -> tuple[list[float], float]:
+    """Max over ranks of the per-step times (the slowest replica bounds the job) and the whole-job
+    throughput: all ranks' steps divided by that time.  Replicas exchange nothing else."""
+    if world > 1:
+        import torch
+
+        t = torch.tensor(ms_local, dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = [float(v) for v in t.cpu()]
+    else:
+        ms = list(ms_local)
+    return ms, world * 1000.0 / ms[0]
+
+
 # ----------------------------------------------------------------------------- engine arm
 
 def run_engine(args, rank: int, world: int) -> dict | None:
@@ -180,12 +194,7 @@ def run_engine(args, rank: int, world: int) -> dict | None:
 
     total_mixed, hv_mixed, clocks, dt_mixed = timed_steps("fp32")
     total_fp64, hv_fp64, _, dt64 = timed_steps("fp64")
-    ms_mixed = total_mixed / K
-    ms_fp64 = total_fp64 / K
-    if world > 1:
-        t = torch.tensor([ms_mixed, ms_fp64], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_mixed, ms_fp64 = float(t[0]), float(t[1])
+    (ms_mixed, ms_fp64), value = aggregate_replicas([total_mixed / K, total_fp64 / K], K, world, dev)
 
     # roofline of the dominant kernel (fused H.v of the step): algorithmic bytes per launch
     s_bytes = torch.empty(0, dtype=dt_mixed).element_size()
@@ -215,7 +224,6 @@ def run_engine(args, rank: int, world: int) -> dict | None:
 
     if rank != 0:
         return None
-    value = world * 1000.0 / ms_mixed
     traffic = ncu_traffic(WORKLOAD)
     return {
         "metric": METRIC,

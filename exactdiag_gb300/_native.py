@@ -48,6 +48,7 @@ SIGNATURES = {
     "ed_batch_lanczos": (_c.c_int, [_c.POINTER(_vp), _c.c_int, _d4, _c.c_int, _c.POINTER(_vp), _c.c_int, _vp,
                                     _c.c_int, _vp]),
     "ed_project_out": (_c.c_int, [_vp, _c.c_int, _vp, _c.c_int, _vp, _vp, _vp]),
+    "ed_project_out_noalloc": (_c.c_int, [_vp, _c.c_int, _vp, _c.c_int, _vp, _vp, _vp]),
     "ed_last_error_string": (_c.c_char_p, []),
 }
 

@@ -262,6 +262,13 @@ int ed_project_out(ed_sector* h, int dtype, const void* basis_dev, int k, void* 
                           s.d_proj.n - 2 * k, (cudaStream_t)stream);
 }
 
+int ed_project_out_noalloc(const ed_sector* h, int dtype, const void* basis_dev, int k, void* w_dev, double* coef_dev,
+                           void* stream) {
+    if (!h || !basis_dev || !w_dev) return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_project_out_noalloc: basis not built");
+    return project_noalloc_launch(h->s, dtype, basis_dev, k, w_dev, coef_dev, (cudaStream_t)stream);
+}
+
 int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const double* omega_dev, int W, double e0,
                           double eta, double norm2, double* out_dev, void* stream) {
     if (!a_dev || !b_dev || !omega_dev || !out_dev) return set_error(ED_ERR_INVALID, "ed_continued_fraction: NULL");

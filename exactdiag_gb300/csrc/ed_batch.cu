@@ -12,6 +12,7 @@
 //
 // Projection (full reorthogonalisation for the lowest-eigenpair solver):
 // w <- w - sum_j <v_j, w> v_j with FP64 dot products.
+#include <mutex>
 #include <vector>
 
 #include "ed_device.cuh"
@@ -475,6 +476,63 @@ int project_launch(const Sector& s, int dtype, const void* V, int k, void* w, do
     case ED_F32: return project_typed<float, false>(s, V, k, w, coef, scratch, nchunks, st);
     case ED_C64: return project_typed<float, true>(s, V, k, w, coef, scratch, nchunks, st);
     default: return set_error(ED_ERR_INVALID, "ed_project_out: dtype");
+    }
+}
+
+// ------------------------------------------------------------ projection without allocation
+//
+// ed_project_out_noalloc: the projection with its scratch (the per-chunk partial dot products and
+// the coefficients) in one fixed device array instead of the per-sector buffer that ed_project_out
+// grows with cudaMalloc.  Every GPU that loads the library holds the array until the process ends.
+// All calls share it, so calls that overlap on the GPU (different streams, or threads) race; the
+// kernels write every partial and coefficient they later read, so nothing needs clearing between
+// calls.
+
+constexpr int kNoAllocMaxVectors = 256;  // largest k accepted
+constexpr int kNoAllocMaxChunks = 256;   // partial sums per vector
+constexpr int64_t kNoAllocScratchDoubles =
+    (int64_t)kNoAllocMaxVectors * kNoAllocMaxChunks * kReduceSlots + 2 * kNoAllocMaxVectors;  // 2.1 MB
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+// Device address of the array for the current device, looked up once per device (host code may
+// not use the symbol itself: on the host it names a stand-in, not device memory).
+static int noalloc_scratch_address(double** out) {
+    static std::mutex mu;
+    static double* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: device ordinal above 63");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetSymbolAddress");
+        addr[dev] = static_cast<double*>(p);
+    }
+    *out = addr[dev];
+    return ED_OK;
+}
+
+int project_noalloc_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef_out,
+                           cudaStream_t st) {
+    if (k < 0) return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: k < 0");
+    if (k > kNoAllocMaxVectors)
+        return set_error(ED_ERR_TOO_LARGE, "ed_project_out_noalloc: k exceeds the fixed scratch (at most 256 vectors)");
+    if (k == 0 || s.view.n == 0) return ED_OK;
+    double* scratch = nullptr;
+    if (int rc = noalloc_scratch_address(&scratch)) return rc;
+    int nchunks = (int)std::min<int64_t>(kNoAllocMaxChunks, (s.view.n + 1023) / 1024);
+    if (nchunks < 1) nchunks = 1;
+    double* partials = scratch;
+    double* coef = coef_out ? coef_out : scratch + (int64_t)kNoAllocMaxVectors * kNoAllocMaxChunks * kReduceSlots;
+    switch (dtype) {
+    case ED_F64: return project_typed<double, false>(s, V, k, w, coef, partials, nchunks, st);
+    case ED_C128: return project_typed<double, true>(s, V, k, w, coef, partials, nchunks, st);
+    case ED_F32: return project_typed<float, false>(s, V, k, w, coef, partials, nchunks, st);
+    case ED_C64: return project_typed<float, true>(s, V, k, w, coef, partials, nchunks, st);
+    default: return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: dtype");
     }
 }
 

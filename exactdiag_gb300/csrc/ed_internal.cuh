@@ -126,6 +126,8 @@ int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights
                          int m, double* coef, int use_graph, cudaStream_t st);
 int project_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef, double* scratch,
                    int64_t scratch_len, cudaStream_t st);
+int project_noalloc_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef_out,
+                           cudaStream_t st);
 int cf_launch(const double* a, const double* b, int m, const double* omega, int W, double e0, double eta,
               double norm2, double* out, cudaStream_t st);
 

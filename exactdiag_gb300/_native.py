@@ -37,6 +37,7 @@ SIGNATURES = {
     "ed_sector_is_real": (_c.c_int, [_vp, _c.POINTER(_c.c_int)]),
     "ed_basis_export": (_c.c_int, [_vp, _vp, _vp, _vp]),
     "ed_hv": (_c.c_int, [_vp, _d4, _c.c_int, _vp, _vp, _vp]),
+    "ed_hv_mode": (_c.c_int, [_vp, _d4, _c.c_int, _vp, _vp, _c.c_int, _vp]),
     "ed_lanczos_step": (_c.c_int, [_vp, _d4, _c.c_int, _vp, _vp, _vp, _vp, _vp]),
     "ed_lanczos_hv": (_c.c_int, [_vp, _d4, _c.c_int, _vp, _vp, _vp, _vp, _vp]),
     "ed_lanczos_update": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _vp]),

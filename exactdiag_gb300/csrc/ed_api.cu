@@ -138,6 +138,7 @@ int ed_basis_build(ed_sector* h, void* stream) {
     if (per_sm <= 0) per_sm = 1;
     if (per_sm > 8) per_sm = 8;
     s.hv_grid = s.num_sms * per_sm;
+    if (int rc2 = build_descriptors(s)) return rc2;
     return single_setup(s);
 }
 
@@ -168,6 +169,7 @@ static bool weights_ok(const double* w, HvWeights& out) {
         // sparse_matrices.py:89 skips |weight| < 1e-6
         out.w[t] = (std::fabs(w[t]) < 1e-6) ? 0.0 : w[t];
     }
+    out.faithful = 0;
     return true;
 }
 
@@ -177,6 +179,18 @@ int ed_hv(const ed_sector* h, const double weights[4], int dtype, const void* x_
     HvWeights w;
     if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_hv: weights");
     if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv: x and y must not alias");
+    return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
+}
+
+int ed_hv_mode(const ed_sector* h, const double weights[4], int dtype, const void* x_dev, void* y_dev, int mode,
+               void* stream) {
+    if (!h || !x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv_mode: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_hv_mode: basis not built");
+    if (mode != 0 && mode != 1) return set_error(ED_ERR_INVALID, "ed_hv_mode: mode must be 0 or 1");
+    HvWeights w;
+    if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_hv_mode: weights");
+    if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv_mode: x and y must not alias");
+    w.faithful = mode;
     return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
 }
 

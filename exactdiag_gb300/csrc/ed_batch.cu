@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kHvThreads)
         double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
         for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
             R hr, hi, xr, xi;
-            hv_row<R, CPLX>(S, tb, w, i, x, hr, hi, xr, xi);
+            hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, hr, hi, xr, xi);
             R yr = hr, yi = hi;
             if (!first) {
                 R pr, pi;

@@ -45,6 +45,58 @@ struct HoleEntry {
     uint8_t pad_;
 };
 
+// ---- per-block descriptors of the fast H.v row (built once per sector) ----------------------
+//
+// Spin configurations are handled as compressed down masks: the down spins of the non-hole
+// sites, packed in increasing site order (bit c = c-th electron).  A group element maps the
+// compressed mask of a state with hole mask h to the compressed mask of its image by swapping
+// the two spins of every doubly occupied rung (mirror, odd product index) and rotating the
+// Ns-bit string left by the number of electrons that wrap around (translation).
+
+constexpr int kMaxCand = 4;    // stabiliser-coset candidates resolved without the orbit walk
+constexpr int kMaxHops = 12;   // 3 hops per hole, up to 4 holes
+
+enum : uint8_t { kModeFree = 0, kModeCand = 1, kModeGeneric = 2, kModeAbsent = 3 };
+
+struct CandParams {
+    uint32_t swap;  // compressed positions c whose spins (c, c+1) the mirror exchanges
+    uint8_t rot;    // left rotation of the Ns-bit compressed mask
+    uint8_t e;      // phase exponent of this group element for the transformed hole mask
+    uint8_t p;      // product index
+    uint8_t pad;
+};
+
+struct HopDesc {
+    uint8_t term;    // 0 tl (leg), 1 tr (rung)
+    uint8_t a, b;    // electron site, hole site
+    uint8_t p, q;    // electron's compressed position before (row mask) and after (new mask) the hop
+    int8_t sign;     // fermion sign (electrons strictly between a and b)
+    uint8_t mode;    // kModeFree / kModeCand / kModeGeneric / kModeAbsent
+    uint8_t ncand;
+    uint32_t keep;   // compressed bits the move leaves in place
+    uint32_t band;   // compressed bits that shift by one position
+    int32_t block;   // target block
+    uint32_t pad;
+    int64_t start, word_off;  // target block rows and bitmap
+    CandParams cand[kMaxCand];
+};
+
+struct BlockDesc {
+    uint32_t hmask;
+    uint8_t mode;        // kModeFree / kModeCand / kModeGeneric
+    uint8_t nhop;
+    uint8_t ncand;
+    uint8_t nwrap;
+    int64_t start, word_off;
+    uint32_t m_rung;     // rung bonds, at the lower compressed position (partner one above)
+    uint32_t m_legadj;   // leg bonds whose middle site is a hole (partner one above)
+    uint32_t m_legd2;    // leg bonds whose middle site is occupied (partner two above)
+    uint8_t wrap[2][2];  // leg bonds across the periodic boundary: compressed positions (lo, hi)
+    uint8_t pad[4];
+    CandParams cand[kMaxCand];  // stabiliser of hmask (exchange targets in kModeCand blocks)
+    HopDesc hop[kMaxHops];
+};
+
 // Read-only view of a built sector, passed to kernels by value.
 struct SectorView {
     int L, N, Nh, Nd, Ns;
@@ -63,6 +115,7 @@ struct SectorView {
     const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word
     const uint32_t* rank_tab;      // [4][Nd+1][256] byte tables of the colex spin rank
     const uint32_t* comb;          // [33][33] comb[k*33+n] = C(n,k)
+    const BlockDesc* desc;         // [n_blocks] fast-row descriptors (null: the orbit-walk row only)
 };
 
 // ---------------------------------------------------------------- bit helpers

@@ -221,6 +221,200 @@ __device__ __forceinline__ void hv_row(const SectorView& S, const HvTables<R>& t
     outi = acci + diag * xii;
 }
 
+
+// ------------------------------------------------------------------ fast row (descriptors)
+
+__device__ __forceinline__ uint32_t rot_ns(uint32_t x, int r, int Ns) {
+    const uint64_t m = (Ns == 32) ? 0xffffffffull : ((1ull << Ns) - 1ull);
+    const uint64_t xx = x;
+    return (uint32_t)(((xx << r) | (xx >> (Ns - r))) & m);
+}
+
+__device__ __forceinline__ uint32_t swap_pairs(uint32_t x, uint32_t m) {
+    const uint32_t t = (x ^ (x >> 1)) & m;
+    return x ^ t ^ (t << 1);
+}
+
+__device__ __forceinline__ uint32_t cand_image(const CandParams& c, uint32_t x, int Ns) {
+    return rot_ns(swap_pairs(x, c.swap), c.rot, Ns);
+}
+
+// Lowest image among the coset candidates: its compressed mask, the number of candidates
+// reaching it (the state's stabiliser order: orbit = 2L / count) and its phase; the state is
+// incompatible with the sector when those candidates disagree in phase (the reference's
+// amplitude tests, symmetry_ladder.h:196-224).
+struct CandResult {
+    uint32_t best;
+    int count, e;
+    bool valid;
+};
+
+__device__ __forceinline__ CandResult resolve_cand(const CandParams* c, int nc, uint32_t x, int Ns) {
+    CandResult r{cand_image(c[0], x, Ns), 1, c[0].e, true};
+    for (int k = 1; k < nc; ++k) {
+        const uint32_t img = cand_image(c[k], x, Ns);
+        if (img < r.best) {
+            r = {img, 1, c[k].e, true};
+        } else if (img == r.best) {
+            ++r.count;
+            if (c[k].e != r.e) r.valid = false;
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ int64_t bitmap_row(const SectorView& S, int64_t word_off, uint32_t r) {
+    const int64_t w = word_off + (r >> 6);
+    const uint64_t bits = S.bitmap[w];
+    const uint64_t bit = 1ull << (r & 63u);
+    if (!(bits & bit)) return -1;
+    return S.word_prefix[w] + __popcll(bits & (bit - 1ull));
+}
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void gather_add(const void* __restrict__ x, int64_t j, R c, int e, const HvTables<R>& tb,
+                                           R& accr, R& acci) {
+    R xr, xi;
+    ld<R, CPLX>(x, j, xr, xi);
+    if constexpr (CPLX) {
+        const R pr = c * tb.cosv[e], pi = c * tb.sinv[e];
+        accr += pr * xr - pi * xi;
+        acci += pr * xi + pi * xr;
+    } else {
+        accr += (e == 0 ? c : -c) * xr;
+    }
+}
+
+// Row i of H via the block descriptor: free blocks move in dense-row space directly (colex rank
+// deltas), hops and non-free blocks go through the precomputed coset permutations.  Rows of
+// blocks marked generic (and the faithful mode) take hv_row.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
+                                            const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
+    const uint64_t key = S.keys[i];
+    const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
+    const HoleEntry hrow = S.holes[hole_rank(h, tb.comb)];
+    const BlockDesc* __restrict__ D = S.desc + hrow.block;
+    const uint8_t mode = D->mode;
+    if (mode == kModeGeneric) {
+        hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+        return;
+    }
+    const int Ns = S.Ns, N = S.N;
+    ld<R, CPLX>(x, i, xir, xii);
+    const uint32_t dc = compress_spins(d, h);
+    const bool row_free = (mode == kModeFree);
+    const int Ni = row_free ? N : (int)S.orbit[i];
+    const R sqNi = tb.sqrtv[Ni];
+    R accr = R(0), acci = R(0);
+    // exchange bonds (jl, jr)
+    const uint32_t dif1 = dc ^ (dc >> 1), dif2 = dc ^ (dc >> 2);
+    const uint32_t mr = D->m_rung & dif1, ma = D->m_legadj & dif1, m2 = D->m_legd2 & dif2;
+    uint32_t wrap_anti = 0;
+    for (int t = 0; t < D->nwrap; ++t)
+        wrap_anti |= (((dc >> D->wrap[t][0]) ^ (dc >> D->wrap[t][1])) & 1u) << t;
+    const R wl = w[2], wr = w[3];
+    const R diag = R(-0.5) * (wr * (R)__popc(mr) + wl * (R)(__popc(ma) + __popc(m2) + __popc(wrap_anti)));
+    if (row_free) {
+        // every neighbour in the block is a representative with orbit 2L and phase 1: y += w/2 x_j
+        const R cr = R(0.5) * wr, cl = R(0.5) * wl;
+#pragma unroll 1
+        for (int kind = 0; kind < 2; ++kind) {
+            uint32_t m = kind == 0 ? mr : ma;
+            const R c = kind == 0 ? cr : cl;
+            if (c == R(0)) continue;
+            while (m) {
+                const int a = __ffs(m) - 1;
+                m &= m - 1u;
+                const int k = __popc(dc & ((1u << a) - 1u));
+                const int64_t delta = tb.comb[k * kCombStride + a];
+                const int64_t j = ((dc >> a) & 1u) ? i + delta : i - delta;
+                gather_add<R, CPLX>(x, j, c, 0, tb, accr, acci);
+            }
+        }
+        if (cl != R(0)) {
+            uint32_t m = m2;
+            while (m) {
+                const int a = __ffs(m) - 1;
+                m &= m - 1u;
+                const int k = __popc(dc & ((1u << a) - 1u));
+                const int mid = (dc >> (a + 1)) & 1u;
+                const int64_t delta = (int64_t)tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+                const int64_t j = ((dc >> a) & 1u) ? i + delta : i - delta;
+                gather_add<R, CPLX>(x, j, cl, 0, tb, accr, acci);
+            }
+            for (int t = 0; t < D->nwrap; ++t) {
+                if (!((wrap_anti >> t) & 1u)) continue;
+                const uint32_t dc2 = dc ^ (1u << D->wrap[t][0]) ^ (1u << D->wrap[t][1]);
+                const int64_t j = D->start + (int64_t)spin_rank(dc2, tb.rank, S.Nd);
+                gather_add<R, CPLX>(x, j, cl, 0, tb, accr, acci);
+            }
+        }
+    } else {
+        // non-free block: each exchange target is resolved through the block's stabiliser
+#pragma unroll 1
+        for (int kind = 0; kind < 4; ++kind) {
+            uint32_t m;
+            int dist;
+            R wt;
+            if (kind == 0) { m = mr; dist = 1; wt = wr; }
+            else if (kind == 1) { m = ma; dist = 1; wt = wl; }
+            else if (kind == 2) { m = m2; dist = 2; wt = wl; }
+            else { m = wrap_anti; dist = 0; wt = wl; }
+            if (wt == R(0)) continue;
+            const R coef = R(0.5) * wt * sqNi;
+            while (m) {
+                const int a = __ffs(m) - 1;
+                m &= m - 1u;
+                const uint32_t flip = dist ? ((1u << a) | (1u << (a + dist)))
+                                           : ((1u << D->wrap[a][0]) | (1u << D->wrap[a][1]));
+                const CandResult cr2 = resolve_cand(D->cand, D->ncand, dc ^ flip, Ns);
+                if (!cr2.valid) continue;
+                const int64_t j = bitmap_row(S, D->word_off, spin_rank(cr2.best, tb.rank, S.Nd));
+                if (j < 0) continue;
+                gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N / cr2.count], cr2.e, tb, accr, acci);
+            }
+        }
+    }
+    // hops (tl, tr)
+    const int nhop = D->nhop;
+#pragma unroll 1
+    for (int t = 0; t < nhop; ++t) {
+        const HopDesc& H = D->hop[t];
+        const R wt = w[H.term];
+        if (wt == R(0) || H.mode == kModeAbsent) continue;
+        const R coef = (H.sign > 0 ? -wt : wt) * sqNi;
+        if (H.mode == kModeGeneric) {
+            const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
+            const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
+            add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
+            continue;
+        }
+        const uint32_t moved = (H.q > H.p) ? ((dc & H.band) >> 1) : ((dc & H.band) << 1);
+        const uint32_t dcm = (dc & H.keep) | moved | (((dc >> H.p) & 1u) << H.q);
+        if (H.mode == kModeFree) {
+            const uint32_t dct = cand_image(H.cand[0], dcm, Ns);
+            const int64_t j = H.start + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+            gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N], H.cand[0].e, tb, accr, acci);
+        } else {
+            const CandResult cr2 = resolve_cand(H.cand, H.ncand, dcm, Ns);
+            if (!cr2.valid) continue;
+            const int64_t j = bitmap_row(S, H.word_off, spin_rank(cr2.best, tb.rank, S.Nd));
+            if (j < 0) continue;
+            gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N / cr2.count], cr2.e, tb, accr, acci);
+        }
+    }
+    outr = accr + diag * xir;
+    outi = acci + diag * xii;
+}
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void hv_row_any(const SectorView& S, const HvTables<R>& tb, const R w[4], int faithful,
+                                           int64_t i, const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
+    if (faithful || S.desc == nullptr) hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+    else hv_row_fast<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+}
+
 template <typename R>
 __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
     uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem);

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kHvThreads) hv_kernel(const SectorView S, HvWe
     const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
         R yr, yi, xr, xi;
-        hv_row<R, CPLX>(S, tb, w, i, x, yr, yi, xr, xi);
+        hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, yr, yi, xr, xi);
         st<R, CPLX>(y, i, yr, yi);
     }
 }

@@ -91,6 +91,7 @@ struct Sector {
     DevBuf<int64_t> d_offs;
     DevBuf<struct BatchChunk> d_chunks;
     DevBuf<int> d_cfirst, d_ccount;
+    DevBuf<BlockDesc> d_desc;    // fast-row descriptors
 };
 
 struct BatchChunk {
@@ -109,7 +110,8 @@ int scan_popcounts(const uint64_t* words, int64_t m, int64_t* prefix, int64_t* t
 
 // ed_hv.cu
 struct HvWeights {
-    double w[4];  // tl, tr, jl, jr; 0 disables a term
+    double w[4];   // tl, tr, jl, jr; 0 disables a term
+    int faithful;  // 1: every term through the reference-faithful orbit walk (self-check path)
 };
 int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st);
 int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev,
@@ -120,6 +122,7 @@ int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext
 int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st);
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
 int single_setup(Sector& s);
+int build_descriptors(Sector& s);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,

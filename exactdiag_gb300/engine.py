@@ -121,6 +121,15 @@ class DeviceSector:
         nat.check("ed_hv", self._lib.ed_hv(self._h, w, code, _ptr(x), _ptr(y), _stream_ptr()))
         return y
 
+    def hv_mode(self, x: torch.Tensor, weights, mode: int, out: torch.Tensor | None = None) -> torch.Tensor:
+        """y = H x with the row algorithm chosen (ed_hv_mode): 0 fast, 1 reference-faithful orbit walk."""
+        code = self._code(x)
+        y = torch.empty_like(x) if out is None else out
+        self._code(y)
+        w = nat.weights_array(weights_tuple(weights))
+        nat.check("ed_hv_mode", self._lib.ed_hv_mode(self._h, w, code, _ptr(x), _ptr(y), int(mode), _stream_ptr()))
+        return y
+
     def lanczos_step(self, weights, v: torch.Tensor, v_prev: torch.Tensor | None, v_next: torch.Tensor,
                      scal: torch.Tensor) -> None:
         """One fused step (ed_lanczos_step); scal is a float64 CUDA tensor of length >= 4."""

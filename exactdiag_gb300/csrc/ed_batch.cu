@@ -52,16 +52,18 @@ __device__ __forceinline__ void* vec_at(void* base, int64_t off) {
 }
 
 template <typename R, bool CPLX>
-__global__ void __launch_bounds__(kHvThreads)
+__global__ void __launch_bounds__(kHvThreads, 3)
     lanczos_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                     const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* vprev, void* other,
                     int first, const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
     extern __shared__ __align__(16) uint8_t smem[];
     const HvTables<R> tb = load_tables<R>(views[0], smem);
     const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
+    __shared__ __align__(16) BlockDesc sdesc;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
         const SectorView S = views[ch.sec];
+        const BlockDesc* staged = W.faithful ? nullptr : stage_desc(S, tb.comb, ch.begin, &sdesc);
         const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
         void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
         const void* yp = first ? nullptr : vec_at<R, CPLX>(vprev, offs[ch.sec]);
@@ -69,7 +71,7 @@ __global__ void __launch_bounds__(kHvThreads)
         double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
         for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
             R hr, hi, xr, xi;
-            hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, hr, hi, xr, xi);
+            hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, hr, hi, xr, xi, staged);
             R yr = hr, yi = hi;
             if (!first) {
                 R pr, pi;

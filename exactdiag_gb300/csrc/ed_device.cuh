@@ -285,25 +285,41 @@ __device__ __forceinline__ void gather_add(const void* __restrict__ x, int64_t j
     }
 }
 
-// Row i of H via the block descriptor: free blocks move in dense-row space directly (colex rank
-// deltas), hops and non-free blocks go through the precomputed coset permutations.  Rows of
-// blocks marked generic (and the faithful mode) take hv_row.
+// Gathers of up to four targets issued together: the addresses first, then the loads, then the
+// products, so a thread keeps several loads in flight (targets with j < 0 contribute nothing).
+template <typename R, bool CPLX>
+__device__ __forceinline__ void gather4(const void* __restrict__ x, const int64_t (&j)[4], const R (&c)[4],
+                                        const int (&e)[4], const HvTables<R>& tb, R& accr, R& acci) {
+    R xr[4], xi[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if (j[u] >= 0) ld<R, CPLX>(x, j[u], xr[u], xi[u]);
+        else xr[u] = xi[u] = R(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if constexpr (CPLX) {
+            const R pr = c[u] * tb.cosv[e[u]], pi = c[u] * tb.sinv[e[u]];
+            accr += pr * xr[u] - pi * xi[u];
+            acci += pr * xi[u] + pi * xr[u];
+        } else {
+            accr += (e[u] == 0 ? c[u] : -c[u]) * xr[u];
+        }
+    }
+}
+
+// Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
+// space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
+// permutations.  Rows of blocks marked generic take hv_row.
 template <typename R, bool CPLX>
 __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
+                                            uint64_t key, const BlockDesc* __restrict__ D,
                                             const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
-    const uint64_t key = S.keys[i];
     const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
-    const HoleEntry hrow = S.holes[hole_rank(h, tb.comb)];
-    const BlockDesc* __restrict__ D = S.desc + hrow.block;
-    const uint8_t mode = D->mode;
-    if (mode == kModeGeneric) {
-        hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
-        return;
-    }
     const int Ns = S.Ns, N = S.N;
     ld<R, CPLX>(x, i, xir, xii);
     const uint32_t dc = compress_spins(d, h);
-    const bool row_free = (mode == kModeFree);
+    const bool row_free = (D->mode == kModeFree);
     const int Ni = row_free ? N : (int)S.orbit[i];
     const R sqNi = tb.sqrtv[Ni];
     R accr = R(0), acci = R(0);
@@ -311,44 +327,66 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
     const uint32_t dif1 = dc ^ (dc >> 1), dif2 = dc ^ (dc >> 2);
     const uint32_t mr = D->m_rung & dif1, ma = D->m_legadj & dif1, m2 = D->m_legd2 & dif2;
     uint32_t wrap_anti = 0;
-    for (int t = 0; t < D->nwrap; ++t)
-        wrap_anti |= (((dc >> D->wrap[t][0]) ^ (dc >> D->wrap[t][1])) & 1u) << t;
+    const int nwrap = D->nwrap;
+    for (int t = 0; t < nwrap; ++t) wrap_anti |= (((dc >> D->wrap[t][0]) ^ (dc >> D->wrap[t][1])) & 1u) << t;
     const R wl = w[2], wr = w[3];
     const R diag = R(-0.5) * (wr * (R)__popc(mr) + wl * (R)(__popc(ma) + __popc(m2) + __popc(wrap_anti)));
+    int64_t jj[4];
+    R cc[4];
+    int ee[4] = {0, 0, 0, 0};
     if (row_free) {
         // every neighbour in the block is a representative with orbit 2L and phase 1: y += w/2 x_j
         const R cr = R(0.5) * wr, cl = R(0.5) * wl;
-#pragma unroll 1
-        for (int kind = 0; kind < 2; ++kind) {
-            uint32_t m = kind == 0 ? mr : ma;
-            const R c = kind == 0 ? cr : cl;
-            if (c == R(0)) continue;
-            while (m) {
-                const int a = __ffs(m) - 1;
-                m &= m - 1u;
-                const int k = __popc(dc & ((1u << a) - 1u));
-                const int64_t delta = tb.comb[k * kCombStride + a];
-                const int64_t j = ((dc >> a) & 1u) ? i + delta : i - delta;
-                gather_add<R, CPLX>(x, j, c, 0, tb, accr, acci);
+        uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
+        while (m1) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (m1) {
+                    const int a = __ffs(m1) - 1;
+                    m1 &= m1 - 1u;
+                    const int k = __popc(dc & ((1u << a) - 1u));
+                    const int64_t delta = tb.comb[k * kCombStride + a];
+                    jj[u] = ((dc >> a) & 1u) ? i + delta : i - delta;
+                    cc[u] = ((mr >> a) & 1u) ? cr : cl;
+                } else {
+                    jj[u] = -1;
+                    cc[u] = R(0);
+                }
             }
+            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
         }
-        if (cl != R(0)) {
-            uint32_t m = m2;
-            while (m) {
-                const int a = __ffs(m) - 1;
-                m &= m - 1u;
-                const int k = __popc(dc & ((1u << a) - 1u));
-                const int mid = (dc >> (a + 1)) & 1u;
-                const int64_t delta = (int64_t)tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
-                const int64_t j = ((dc >> a) & 1u) ? i + delta : i - delta;
-                gather_add<R, CPLX>(x, j, cl, 0, tb, accr, acci);
+        uint32_t mm = cl != R(0) ? m2 : 0u;
+        while (mm) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (mm) {
+                    const int a = __ffs(mm) - 1;
+                    mm &= mm - 1u;
+                    const int k = __popc(dc & ((1u << a) - 1u));
+                    const int mid = (dc >> (a + 1)) & 1u;
+                    const int64_t delta =
+                        (int64_t)tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+                    jj[u] = ((dc >> a) & 1u) ? i + delta : i - delta;
+                    cc[u] = cl;
+                } else {
+                    jj[u] = -1;
+                    cc[u] = R(0);
+                }
             }
-            for (int t = 0; t < D->nwrap; ++t) {
-                if (!((wrap_anti >> t) & 1u)) continue;
-                const uint32_t dc2 = dc ^ (1u << D->wrap[t][0]) ^ (1u << D->wrap[t][1]);
-                const int64_t j = D->start + (int64_t)spin_rank(dc2, tb.rank, S.Nd);
-                gather_add<R, CPLX>(x, j, cl, 0, tb, accr, acci);
+            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
+        }
+        if (cl != R(0) && wrap_anti) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                jj[u] = -1;
+                cc[u] = R(0);
+                if (u < 2 && ((wrap_anti >> u) & 1u)) {
+                    const uint32_t dc2 = dc ^ (1u << D->wrap[u][0]) ^ (1u << D->wrap[u][1]);
+                    jj[u] = D->start + (int64_t)spin_rank(dc2, tb.rank, S.Nd);
+                    cc[u] = cl;
+                }
             }
+            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
         }
     } else {
         // non-free block: each exchange target is resolved through the block's stabiliser
@@ -376,43 +414,84 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
             }
         }
     }
-    // hops (tl, tr)
+    // hops (tl, tr), four at a time
     const int nhop = D->nhop;
 #pragma unroll 1
-    for (int t = 0; t < nhop; ++t) {
-        const HopDesc& H = D->hop[t];
-        const R wt = w[H.term];
-        if (wt == R(0) || H.mode == kModeAbsent) continue;
-        const R coef = (H.sign > 0 ? -wt : wt) * sqNi;
-        if (H.mode == kModeGeneric) {
-            const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
-            const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
-            add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
-            continue;
+    for (int t0 = 0; t0 < nhop; t0 += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            jj[u] = -1;
+            cc[u] = R(0);
+            ee[u] = 0;
+            const int t = t0 + u;
+            if (t >= nhop) continue;
+            const HopDesc& H = D->hop[t];
+            const R wt = H.term ? w[1] : w[0];
+            if (wt == R(0) || H.mode == kModeAbsent) continue;
+            const R coef = (H.sign > 0 ? -wt : wt) * sqNi;
+            if (H.mode == kModeGeneric) {
+                const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
+                const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
+                add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
+                continue;
+            }
+            const uint32_t moved = (H.q > H.p) ? ((dc & H.band) >> 1) : ((dc & H.band) << 1);
+            const uint32_t dcm = (dc & H.keep) | moved | (((dc >> H.p) & 1u) << H.q);
+            if (H.mode == kModeFree) {
+                const uint32_t dct = cand_image(H.cand[0], dcm, Ns);
+                jj[u] = H.start + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+                cc[u] = coef * tb.rsqrtv[N];
+                ee[u] = H.cand[0].e;
+            } else {
+                const CandResult cr2 = resolve_cand(H.cand, H.ncand, dcm, Ns);
+                if (!cr2.valid) continue;
+                const int64_t j = bitmap_row(S, H.word_off, spin_rank(cr2.best, tb.rank, S.Nd));
+                if (j < 0) continue;
+                jj[u] = j;
+                cc[u] = coef * tb.rsqrtv[N / cr2.count];
+                ee[u] = cr2.e;
+            }
         }
-        const uint32_t moved = (H.q > H.p) ? ((dc & H.band) >> 1) : ((dc & H.band) << 1);
-        const uint32_t dcm = (dc & H.keep) | moved | (((dc >> H.p) & 1u) << H.q);
-        if (H.mode == kModeFree) {
-            const uint32_t dct = cand_image(H.cand[0], dcm, Ns);
-            const int64_t j = H.start + (int64_t)spin_rank(dct, tb.rank, S.Nd);
-            gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N], H.cand[0].e, tb, accr, acci);
-        } else {
-            const CandResult cr2 = resolve_cand(H.cand, H.ncand, dcm, Ns);
-            if (!cr2.valid) continue;
-            const int64_t j = bitmap_row(S, H.word_off, spin_rank(cr2.best, tb.rank, S.Nd));
-            if (j < 0) continue;
-            gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N / cr2.count], cr2.e, tb, accr, acci);
-        }
+        gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
     }
     outr = accr + diag * xir;
     outi = acci + diag * xii;
 }
 
+// Descriptor of the row's block: the chunk's staged copy when the hole masks agree, else the table.
+__device__ __forceinline__ const BlockDesc* row_desc(const SectorView& S, const uint32_t* comb, uint32_t h,
+                                                     const BlockDesc* staged) {
+    if (staged && staged->hmask == h) return staged;
+    return S.desc + S.holes[hole_rank(h, comb)].block;
+}
+
 template <typename R, bool CPLX>
 __device__ __forceinline__ void hv_row_any(const SectorView& S, const HvTables<R>& tb, const R w[4], int faithful,
-                                           int64_t i, const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
-    if (faithful || S.desc == nullptr) hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
-    else hv_row_fast<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+                                           int64_t i, const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii,
+                                           const BlockDesc* staged = nullptr) {
+    if (faithful || S.desc == nullptr) {
+        hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+        return;
+    }
+    const uint64_t key = S.keys[i];
+    const BlockDesc* D = row_desc(S, tb.comb, (uint32_t)(key >> 32), staged);
+    if (D->mode == kModeGeneric) hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
+    else hv_row_fast<R, CPLX>(S, tb, w, i, key, D, x, outr, outi, xir, xii);
+}
+
+// Stage the block descriptor of row `first` in shared memory (all threads of the CTA call this).
+__device__ __forceinline__ const BlockDesc* stage_desc(const SectorView& S, const uint32_t* comb, int64_t first,
+                                                       BlockDesc* sdesc) {
+    if (S.desc == nullptr) return nullptr;
+    __syncthreads();  // the previous chunk's rows are done with sdesc
+    const uint32_t h = (uint32_t)(S.keys[first] >> 32);
+    const BlockDesc* src = S.desc + S.holes[hole_rank(h, comb)].block;
+    const int words = (int)(sizeof(BlockDesc) / sizeof(uint32_t));
+    const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d32 = reinterpret_cast<uint32_t*>(sdesc);
+    for (int t = threadIdx.x; t < words; t += blockDim.x) d32[t] = s32[t];
+    __syncthreads();
+    return sdesc;
 }
 
 template <typename R>

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kHvThreads, 3)
         void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
         const void* yp = first ? nullptr : vec_at<R, CPLX>(vprev, offs[ch.sec]);
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
-        double acc[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
+        Accum<R> acc[kReduceSlots];
         for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
             R hr, hi, xr, xi;
             hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, hr, hi, xr, xi, staged);
@@ -77,16 +77,22 @@ __global__ void __launch_bounds__(kHvThreads, 3)
                 R pr, pi;
                 ld<R, CPLX>(yp, i, pr, pi);  // v_{k-1}; may be the same buffer as y (read before written)
                 yr -= beta * pr;
-                yi -= beta * pi;
+                if constexpr (CPLX) yi -= beta * pi;
             }
             st<R, CPLX>(y, i, yr, yi);
-            const double dxr = xr, dxi = xi, dyr = yr, dyi = yi;
-            acc[0] = fma(dxr, (double)hr, fma(dxi, (double)hi, acc[0]));
-            acc[1] = fma(dyr, dyr, fma(dyi, dyi, acc[1]));
-            acc[2] = fma(dxr, dyr, fma(dxi, dyi, acc[2]));
-            acc[3] = fma(dxr, dxr, fma(dxi, dxi, acc[3]));
+            acc[0].add_prod(xr, hr);
+            acc[1].add_prod(yr, yr);
+            acc[2].add_prod(xr, yr);
+            acc[3].add_prod(xr, xr);
+            if constexpr (CPLX) {
+                acc[0].add_prod(xi, hi);
+                acc[1].add_prod(yi, yi);
+                acc[2].add_prod(xi, yi);
+                acc[3].add_prod(xi, xi);
+            }
         }
-        chunk_reduce(acc, partials + (int64_t)c * kReduceSlots);
+        double tot[kReduceSlots] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
+        chunk_reduce(tot, partials + (int64_t)c * kReduceSlots);
     }
 }
 

@@ -5,6 +5,37 @@
 
 namespace ed {
 
+// Per-thread sums of products for the Lanczos dot products.  FP64 vectors: FP64 fused
+// multiply-adds.  FP32 vectors: each product is split exactly into a float pair (fma gives the
+// rounding error) and added with Knuth's TwoSum into a float-float sum, so a thread's partial
+// sum carries about 48 bits; the CTA and sector reductions then run in FP64.  This keeps the
+// FP64 units (1/64 of the FP32 rate on this part) off the per-row path.
+template <typename R>
+struct Accum;
+
+template <>
+struct Accum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct Accum<float> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        // explicit round-to-nearest operations: no contraction may merge the product into the sum
+        const float p = __fmul_rn(a, b);
+        const float pe = __fmaf_rn(a, b, -p);
+        const float t = __fadd_rn(hi, p);
+        const float bv = __fsub_rn(t, hi);
+        const float te = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bv)), __fsub_rn(p, bv));
+        lo = __fadd_rn(lo, __fadd_rn(te, pe));
+        hi = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 template <typename R>
 struct HvTables {
     const uint32_t* rank;  // shared
@@ -308,6 +339,25 @@ __device__ __forceinline__ void gather4(const void* __restrict__ x, const int64_
     }
 }
 
+// Four gathers from one block: x_blk points at the block's first row, offsets are 32-bit rows
+// inside it; slots whose bit in `live` is clear contribute nothing.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void gather4_block(const typename Vec<R, CPLX>::T* __restrict__ xb,
+                                              const uint32_t (&off)[4], unsigned live, const R (&c)[4],
+                                              R& accr, R& acci) {
+    R xr[4], xi[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if ((live >> u) & 1u) ld<R, CPLX>(xb, off[u], xr[u], xi[u]);
+        else xr[u] = xi[u] = R(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        accr += c[u] * xr[u];
+        if constexpr (CPLX) acci += c[u] * xi[u];
+    }
+}
+
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
@@ -335,58 +385,66 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
     R cc[4];
     int ee[4] = {0, 0, 0, 0};
     if (row_free) {
-        // every neighbour in the block is a representative with orbit 2L and phase 1: y += w/2 x_j
+        // every neighbour in the block is a representative with orbit 2L and phase 1: y += w/2 x_j,
+        // at row i + delta of the same block (32-bit offsets from the block's first row)
         const R cr = R(0.5) * wr, cl = R(0.5) * wl;
+        const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(x) + D->start;
+        const uint32_t ri = (uint32_t)(i - D->start);
+        uint32_t off[4];
+        R cb[4];
         uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
         while (m1) {
+            unsigned live = 0;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
+                off[u] = ri;
+                cb[u] = R(0);
                 if (m1) {
                     const int a = __ffs(m1) - 1;
                     m1 &= m1 - 1u;
                     const int k = __popc(dc & ((1u << a) - 1u));
-                    const int64_t delta = tb.comb[k * kCombStride + a];
-                    jj[u] = ((dc >> a) & 1u) ? i + delta : i - delta;
-                    cc[u] = ((mr >> a) & 1u) ? cr : cl;
-                } else {
-                    jj[u] = -1;
-                    cc[u] = R(0);
+                    const uint32_t delta = tb.comb[k * kCombStride + a];
+                    off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
+                    cb[u] = ((mr >> a) & 1u) ? cr : cl;
+                    live |= 1u << u;
                 }
             }
-            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
+            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
         }
         uint32_t mm = cl != R(0) ? m2 : 0u;
         while (mm) {
+            unsigned live = 0;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
+                off[u] = ri;
+                cb[u] = R(0);
                 if (mm) {
                     const int a = __ffs(mm) - 1;
                     mm &= mm - 1u;
                     const int k = __popc(dc & ((1u << a) - 1u));
                     const int mid = (dc >> (a + 1)) & 1u;
-                    const int64_t delta =
-                        (int64_t)tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
-                    jj[u] = ((dc >> a) & 1u) ? i + delta : i - delta;
-                    cc[u] = cl;
-                } else {
-                    jj[u] = -1;
-                    cc[u] = R(0);
+                    const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+                    off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
+                    cb[u] = cl;
+                    live |= 1u << u;
                 }
             }
-            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
+            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
         }
         if (cl != R(0) && wrap_anti) {
+            unsigned live = 0;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                jj[u] = -1;
-                cc[u] = R(0);
+                off[u] = ri;
+                cb[u] = R(0);
                 if (u < 2 && ((wrap_anti >> u) & 1u)) {
                     const uint32_t dc2 = dc ^ (1u << D->wrap[u][0]) ^ (1u << D->wrap[u][1]);
-                    jj[u] = D->start + (int64_t)spin_rank(dc2, tb.rank, S.Nd);
-                    cc[u] = cl;
+                    off[u] = spin_rank(dc2, tb.rank, S.Nd);
+                    cb[u] = cl;
+                    live |= 1u << u;
                 }
             }
-            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
+            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
         }
     } else {
         // non-free block: each exchange target is resolved through the block's stabiliser

@@ -154,8 +154,13 @@ def run_engine(args, rank: int, world: int) -> dict | None:
     n = sec.n
     K, W = args.steps, args.warmup
 
+    from exactdiag_gb300 import autotune
+
+    tuned = {}
+
     def timed_steps(precision: str):
         dt = sec.dtype(precision)
+        tuned[precision] = autotune.tune(sec, WEIGHTS, dt)
         rng = np.random.default_rng(0)
         v0 = torch.as_tensor(rng.uniform(-1, 1, n), device=dev).to(dt)
         buf = [v0.clone(), torch.zeros_like(v0)]
@@ -209,6 +214,7 @@ def run_engine(args, rank: int, world: int) -> dict | None:
     # per step with the step's (a_k, b_{k+1}) read back to the host
     e2e = None
     if rank == 0:
+        autotune.set_launch(sec, tuned["fp32"]["min_ctas_per_sm"], tuned["fp32"]["ctas_per_sm"])
         e2e = e2e_steps(sec, K, dt_mixed)
 
     energy = {}
@@ -255,6 +261,7 @@ def run_engine(args, rank: int, world: int) -> dict | None:
             "hv_gbs_fp64": hv64_gbs,
             "bytes_per_row_mixed": bytes_per_row,
             "parallelism": "replicas" if world > 1 else "single GPU",
+            "launch": {p: {k: v for k, v in r.items() if k != "candidates"} for p, r in tuned.items()},
             **energy,
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

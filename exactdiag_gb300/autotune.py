@@ -1,0 +1,109 @@
+"""Launch-configuration autotuner of the fused Lanczos step.
+
+For a sector shape (L, Nh, Nd, real/complex) and vector dtype it times a few steps for each
+candidate (compiled register variant x persistent grid size, ed_sector_set_launch) and keeps the
+fastest.  Results are cached as JSON keyed by GPU name and shape, so later runs apply the choice
+without timing.  The choice changes only how chunks map onto CTAs: every chunk's partial sums are
+reduced in a fixed order, so results are bitwise identical across candidates.
+
+Cache file: $EXACTDIAG_GB300_AUTOTUNE, else ~/.cache/exactdiag_gb300/autotune.json.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import pathlib
+
+import numpy as np
+import torch
+
+from exactdiag_gb300 import _native as nat
+from exactdiag_gb300.engine import DeviceSector
+
+CANDIDATES = ((3, 0), (4, 0), (3, 2), (4, 3))
+
+
+def cache_path() -> pathlib.Path:
+    env = os.environ.get("EXACTDIAG_GB300_AUTOTUNE")
+    if env:
+        return pathlib.Path(env)
+    return pathlib.Path.home() / ".cache" / "exactdiag_gb300" / "autotune.json"
+
+
+def _key(sector: DeviceSector, dtype: torch.dtype) -> str:
+    k = sector.key
+    name = torch.cuda.get_device_name(sector.device)
+    kind = "real" if sector.is_real else "complex"
+    return f"{name}|L{k.num_rungs}|Nh{k.num_holes}|Nd{k.num_down_spins}|{kind}|{str(dtype).replace('torch.', '')}"
+
+
+def _load() -> dict:
+    p = cache_path()
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _save(cache: dict) -> None:
+    p = cache_path()
+    try:
+        p.parent.mkdir(parents=True, exist_ok=True)
+        tmp = p.with_suffix(".tmp")
+        tmp.write_text(json.dumps(cache, indent=1, sort_keys=True))
+        os.replace(tmp, p)
+    except OSError:
+        pass  # a read-only home is not an error: the choice is still applied for this process
+
+
+def set_launch(sector: DeviceSector, min_ctas: int, ctas: int) -> None:
+    nat.check("ed_sector_set_launch", sector._lib.ed_sector_set_launch(sector.handle, int(min_ctas), int(ctas)))
+
+
+def get_launch(sector: DeviceSector) -> tuple[int, int]:
+    a, g = ctypes.c_int(), ctypes.c_int()
+    nat.check("ed_sector_get_launch", sector._lib.ed_sector_get_launch(sector.handle, ctypes.byref(a),
+                                                                       ctypes.byref(g)))
+    return a.value, g.value
+
+
+def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_cache: bool = True) -> dict:
+    """Apply the fastest launch configuration for this sector shape; returns the record used."""
+    key = _key(sector, dtype)
+    cache = _load() if use_cache else {}
+    if key in cache:
+        rec = cache[key]
+        set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+        return dict(rec, cached=True)
+    n = sector.n
+    v = torch.as_tensor(np.random.default_rng(3).uniform(-1, 1, n), device=sector.device).to(dtype)
+    buf = [v.clone(), torch.zeros_like(v)]
+    scal = torch.zeros(2 * (steps + 2) + 4, dtype=torch.float64, device=sector.device)
+    norm = torch.zeros(1, dtype=torch.float64, device=sector.device)
+    sector.normalize(buf[0], norm)
+    timings = {}
+    for minb, ctas in CANDIDATES:
+        try:
+            set_launch(sector, minb, ctas)
+        except nat.EngineError:
+            continue
+        for k in range(steps + 1):
+            if k == 1:
+                torch.cuda.synchronize()
+                start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                start.record()
+            other = buf[(k + 1) % 2]
+            sector.lanczos_step(weights, buf[k % 2], other if k else None, other, scal[2 * k: 2 * k + 4])
+        stop.record()
+        torch.cuda.synchronize()
+        timings[(minb, ctas)] = start.elapsed_time(stop) / steps
+    best = min(timings, key=timings.get)
+    set_launch(sector, *best)
+    rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "ms_per_step": timings[best],
+           "grid": get_launch(sector)[1], "candidates": {f"{a},{b}": t for (a, b), t in timings.items()}}
+    cache[key] = rec
+    if use_cache:
+        _save(cache)
+    return dict(rec, cached=False)

@@ -85,11 +85,21 @@ int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out) {
     }
     cudaGetDevice(&s.device);
     cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, s.device);
-    // colex spin-rank byte tables: T[c][k][byte]
-    std::vector<uint32_t> tab((size_t)4 * (Nd + 1) * 256, 0u);
+    // colex spin-rank byte tables, compact: chunk c has 2^w entries per k, w = min(8, Ns - 8c)
+    const int Ns = N - Nh;
+    uint32_t words = 0;
+    for (int c = 0; c < 4; ++c) {
+        int wbits = Ns - 8 * c;
+        wbits = wbits < 0 ? 0 : (wbits > 8 ? 8 : wbits);
+        V.rk_sh[c] = (uint32_t)wbits;
+        V.rk_off[c] = words;
+        words += (uint32_t)(Nd + 1) << wbits;
+    }
+    V.rank_words = (int)words;
+    std::vector<uint32_t> tab(words, 0u);
     for (int c = 0; c < 4; ++c)
         for (int k = 0; k <= Nd; ++k)
-            for (int byte = 0; byte < 256; ++byte) {
+            for (int byte = 0; byte < (1 << V.rk_sh[c]); ++byte) {
                 uint32_t r = 0;
                 int j = 0;
                 for (int b = 0; b < 8; ++b)
@@ -98,7 +108,7 @@ int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out) {
                         const int nn = 8 * c + b, kk = k + j;
                         if (kk <= kMaxN) r += comb[kk][nn];
                     }
-                tab[((size_t)c * (Nd + 1) + k) * 256 + byte] = r;
+                tab[V.rk_off[c] + ((uint32_t)k << V.rk_sh[c]) + byte] = r;
             }
     if (!s.d_comb.alloc(kCombStride * kCombStride) || !s.d_rank_tab.alloc((int64_t)tab.size())) {
         delete h;
@@ -139,7 +149,21 @@ int ed_basis_build(ed_sector* h, void* stream) {
     if (per_sm > 8) per_sm = 8;
     s.hv_grid = s.num_sms * per_sm;
     if (int rc2 = build_descriptors(s)) return rc2;
-    return single_setup(s);
+    if (int rc3 = single_setup(s)) return rc3;
+    return set_launch(s, 3, 0);
+}
+
+int ed_sector_set_launch(ed_sector* h, int min_ctas_per_sm, int ctas_per_sm) {
+    if (!h) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: NULL sector");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_set_launch: basis not built");
+    return set_launch(h->s, min_ctas_per_sm, ctas_per_sm);
+}
+
+int ed_sector_get_launch(const ed_sector* h, int* min_ctas_per_sm, int* grid) {
+    if (!h || !min_ctas_per_sm || !grid) return set_error(ED_ERR_INVALID, "ed_sector_get_launch: NULL argument");
+    *min_ctas_per_sm = h->s.hv_minb;
+    *grid = h->s.hv_grid;
+    return ED_OK;
 }
 
 int ed_basis_size(const ed_sector* h, int64_t* n) {

@@ -287,14 +287,20 @@ __global__ void export_sparse_kernel(SectorView S, uint64_t n_spin, int64_t* __r
     extern __shared__ uint32_t s_tab[];
     uint32_t* s_comb = s_tab;
     uint32_t* s_rank = s_tab + kCombStride * kCombStride;
-    const int tab_words = 4 * (S.Nd + 1) * 256;
+    const int tab_words = S.rank_words;
     for (int i = threadIdx.x; i < kCombStride * kCombStride; i += blockDim.x) s_comb[i] = S.comb[i];
     for (int i = threadIdx.x; i < tab_words; i += blockDim.x) s_rank[i] = S.rank_tab[i];
     __syncthreads();
+    RankTab rt;
+    rt.T = s_rank;
+    for (int c = 0; c < 4; ++c) {
+        rt.off[c] = S.rk_off[c];
+        rt.sh[c] = S.rk_sh[c];
+    }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t key = S.keys[i];
         const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
-        sparse[i] = (int64_t)hole_rank(h, s_comb) * (int64_t)n_spin + spin_rank(compress_spins(d, h), s_rank, S.Nd);
+        sparse[i] = (int64_t)hole_rank(h, s_comb) * (int64_t)n_spin + spin_rank(compress_spins(d, h), rt, S.Nd);
         orbit_out[i] = S.orbit[i];
     }
 }
@@ -388,7 +394,7 @@ int basis_build(Sector& s, cudaStream_t st) {
 int basis_export(Sector& s, int64_t* sparse_dev, int32_t* orbit_dev, cudaStream_t st) {
     const SectorView& V = s.view;
     if (V.n == 0) return ED_OK;
-    const size_t smem = (kCombStride * kCombStride + 4 * (V.Nd + 1) * 256) * sizeof(uint32_t);
+    const size_t smem = (kCombStride * kCombStride + V.rank_words) * sizeof(uint32_t);
     export_sparse_kernel<<<grid_for(V.n, 256, s.num_sms), 256, smem, st>>>(V, s.n_spin, sparse_dev, orbit_dev);
     ED_CHECK_LAUNCH("export_sparse_kernel");
     return ED_OK;

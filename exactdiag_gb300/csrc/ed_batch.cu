@@ -51,8 +51,8 @@ __device__ __forceinline__ void* vec_at(void* base, int64_t off) {
     return reinterpret_cast<typename Vec<R, CPLX>::T*>(base) + off;
 }
 
-template <typename R, bool CPLX>
-__global__ void __launch_bounds__(kHvThreads, 3)
+template <typename R, bool CPLX, int MINB>
+__global__ void __launch_bounds__(kHvThreads, MINB)
     lanczos_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                     const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* vprev, void* other,
                     int first, const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
@@ -234,7 +234,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
             cudaMemcpyAsync(buf0.p + hoffs[s] * esz, v0[s], hviews[s].n * esz, cudaMemcpyDeviceToDevice, st);
     const int grid = std::min(nchunks, secs[0]->hv_grid > 0 ? secs[0]->hv_grid : secs[0]->num_sms * 3);
     const size_t smem = hv_smem_bytes(hviews[0], sizeof(R));
-    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // start vectors: |v0| and normalisation
     norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
     lanczos_scalars_kernel<<<nsec, 256, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1, stride - 1);
@@ -256,7 +256,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     for (int k = 0; k < m; ++k) {
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
-        lanczos_hv_kernel<R, CPLX><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
+        lanczos_hv_kernel<R, CPLX, 3><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
                                                                     other, k == 0, coef, stride, k, partials.p);
         lanczos_scalars_kernel<<<nsec, 256, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
         lanczos_update_kernel<R, CPLX><<<grid, 256, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0,
@@ -332,17 +332,54 @@ static bool dtype_fits(const Sector& s, int dtype) {
 
 static int step_grid(const Sector& s) { return std::max(1, std::min(s.n_chunks, s.hv_grid)); }
 
-template <typename R, bool CPLX>
-static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
-                           double* scal, cudaStream_t st) {
+template <typename R, bool CPLX, int MINB>
+static int single_hv_variant(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
+                             double* scal, cudaStream_t st) {
     const size_t smem = hv_smem_bytes(s.view, sizeof(R));
-    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    lanczos_hv_kernel<R, CPLX><<<step_grid(s), kHvThreads, smem, st>>>(
+    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lanczos_hv_kernel<R, CPLX, MINB><<<step_grid(s), kHvThreads, smem, st>>>(
         s.d_self.p, s.d_offs.p, s.d_chunks.p, s.n_chunks, w, const_cast<void*>(v), const_cast<void*>(vprev), vnext,
         vprev == nullptr, scal, 0, 0, s.d_partials.p);
     ED_CHECK_LAUNCH("lanczos_hv_kernel");
+    return ED_OK;
+}
+
+template <typename R, bool CPLX>
+static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
+                           double* scal, cudaStream_t st) {
+    const int rc = (s.hv_minb == 4) ? single_hv_variant<R, CPLX, 4>(s, w, v, vprev, vnext, scal, st)
+                                    : single_hv_variant<R, CPLX, 3>(s, w, v, vprev, vnext, scal, st);
+    if (rc != ED_OK) return rc;
     lanczos_scalars_kernel<<<1, 256, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
     ED_CHECK_LAUNCH("lanczos_scalars_kernel");
+    return ED_OK;
+}
+
+// Resident CTAs per SM of the fused step kernel for a sector, per launch variant.
+template <int MINB>
+static int step_occupancy(const SectorView& V) {
+    const size_t smem = hv_smem_bytes(V, sizeof(float));
+    cudaFuncSetAttribute(lanczos_hv_kernel<float, false, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_hv_kernel<float, false, MINB>, kHvThreads,
+                                                      smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return per_sm > 0 ? per_sm : 1;
+}
+
+int set_launch(Sector& s, int minb, int ctas_per_sm) {
+    if (minb != 3 && minb != 4) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: variant must be 3 or 4");
+    const int occ = (minb == 4) ? step_occupancy<4>(s.view) : step_occupancy<3>(s.view);
+    if (ctas_per_sm < 0 || ctas_per_sm > 8) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: ctas_per_sm");
+    const int per_sm = (ctas_per_sm == 0 || ctas_per_sm > occ) ? occ : ctas_per_sm;
+    const int grid = s.num_sms * per_sm;
+    const int64_t slots = (int64_t)std::max(s.n_chunks, grid) * kReduceSlots;
+    if (s.d_partials.n < slots && !s.d_partials.alloc(slots)) return set_error(ED_ERR_NOMEM, "reduction scratch");
+    s.hv_minb = minb;
+    s.hv_grid = grid;
     return ED_OK;
 }
 

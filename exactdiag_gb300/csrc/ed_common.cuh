@@ -113,7 +113,10 @@ struct SectorView {
     const uint8_t* orbit;          // [n] orbit size (num_sparse_states_in_dense)
     const uint64_t* bitmap;        // candidate bitmaps of non-free blocks
     const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word
-    const uint32_t* rank_tab;      // [4][Nd+1][256] byte tables of the colex spin rank
+    const uint32_t* rank_tab;      // byte tables of the colex spin rank (compact layout, see RankTab)
+    uint32_t rk_off[4];            // first word of byte-chunk c's table
+    uint32_t rk_sh[4];             // log2 of the entries per k of chunk c (8, or fewer for the top chunk)
+    int rank_words;                // words of rank_tab
     const uint32_t* comb;          // [33][33] comb[k*33+n] = C(n,k)
     const BlockDesc* desc;         // [n_blocks] fast-row descriptors (null: the orbit-walk row only)
 };
@@ -173,16 +176,23 @@ __host__ __device__ __forceinline__ uint32_t compress_spins(uint32_t d, uint32_t
     return d;
 }
 
-// Colex rank of a compressed down mask from byte tables:
-// T[(c*(Nd+1) + k)*256 + byte] = sum over the set bits of `byte` (j-th from
-// the bottom) of C(8c + bitpos, k + j).
-__host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const uint32_t* T, int Nd) {
+// Colex rank of a compressed down mask from byte tables.  Chunk c covers compressed bits
+// 8c..8c+7; with k set bits below the chunk, T[off[c] + (k << sh[c]) + byte] is the sum over
+// the chunk's set bits (j-th from the bottom) of C(8c + bitpos, k + j).  The top chunk holds only
+// 2^(Ns - 8c) entries per k.
+struct RankTab {
+    const uint32_t* T;
+    uint32_t off[4];
+    uint32_t sh[4];
+};
+
+__host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const RankTab& R, int Nd) {
     uint32_t r = 0;
     int k = 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         const uint32_t byte = (dc >> (8 * c)) & 255u;
-        r += T[(c * (Nd + 1) + k) * 256 + byte];
+        r += R.T[R.off[c] + ((uint32_t)k << R.sh[c]) + byte];
         k += popc32(byte);
         if (k > Nd) k = Nd;
     }

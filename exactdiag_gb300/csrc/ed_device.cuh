@@ -38,7 +38,7 @@ struct Accum<float> {
 
 template <typename R>
 struct HvTables {
-    const uint32_t* rank;  // shared
+    RankTab rank;          // shared
     const uint32_t* comb;  // shared
     const R* cosv;         // cos(pi e / L), e in [0, 2L)
     const R* sinv;         // +sin(pi e / L): conj(u^e) = cos + i sin
@@ -94,7 +94,7 @@ __device__ __forceinline__ void st(void* v, int64_t j, R re, R im) {
 // Dense row of representative spin mask `dr` in block B, or -1 when the
 // configuration is not a representative of the sector.
 __device__ __forceinline__ int64_t dense_in_block(const SectorView& S, const BlockInfo& B, uint32_t dr,
-                                                  const uint32_t* rank_tab) {
+                                                  const RankTab& rank_tab) {
     const uint32_t r = spin_rank(compress_spins(dr, B.hmask), rank_tab, S.Nd);
     if (B.flags & kBlockFree) return B.start + (int64_t)r;
     const int64_t w = B.word_off + (r >> 6);
@@ -114,7 +114,7 @@ struct Resolved {
 // Representative of the configuration (h2, d2) in sector S: dense row, orbit
 // size and phase exponent of the lowest image
 // (general/symmetry.h:97-126 then general/basis_indexing.h:152-168).
-__device__ __forceinline__ Resolved resolve(const SectorView& S, const uint32_t* rank_tab, const uint32_t* comb,
+__device__ __forceinline__ Resolved resolve(const SectorView& S, const RankTab& rank_tab, const uint32_t* comb,
                                             uint32_t h2, uint32_t d2) {
     const HoleEntry he = S.holes[hole_rank(h2, comb)];
     if (he.block < 0) return {-1, 0, 0, 0};
@@ -555,8 +555,8 @@ __device__ __forceinline__ const BlockDesc* stage_desc(const SectorView& S, cons
 template <typename R>
 __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
     uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem);
-    const int tab_words = 4 * (S.Nd + 1) * 256;
-    uint32_t* s_comb = s_rank + tab_words;
+    const int tab_words = S.rank_words;
+    uint32_t* s_comb = s_rank + ((tab_words + 1) & ~1);
     R* s_f = reinterpret_cast<R*>(s_comb + kCombStride * kCombStride + 1);  // 8-byte aligned (odd count + 1)
     R* s_cos = s_f;
     R* s_sin = s_f + 64;
@@ -575,11 +575,19 @@ __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
         s_rsqrt[i] = i ? (R)(1.0 / sqrt((double)i)) : R(0);
     }
     __syncthreads();
-    return HvTables<R>{s_rank, s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
+    RankTab rt;
+    rt.T = s_rank;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        rt.off[c] = S.rk_off[c];
+        rt.sh[c] = S.rk_sh[c];
+    }
+    return HvTables<R>{rt, s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
 }
 
 inline size_t hv_smem_bytes(const SectorView& S, size_t real_size) {
-    return (4 * (S.Nd + 1) * 256 + kCombStride * kCombStride + 1) * sizeof(uint32_t) + (64 + 64 + 33 + 33) * real_size;
+    return (((S.rank_words + 1) & ~1) + kCombStride * kCombStride + 1) * sizeof(uint32_t) +
+           (64 + 64 + 33 + 33) * real_size;
 }
 
 }  // namespace ed

@@ -75,6 +75,7 @@ struct Sector {
     int device = 0;
     int num_sms = 152;
     int hv_grid = 0;             // persistent grid of the H.v kernels
+    int hv_minb = 3;             // launch variant of the fused step kernel (minimum resident CTAs per SM)
     DevBuf<uint32_t> d_comb;     // [33][33]
     DevBuf<uint32_t> d_rank_tab; // [4][Nd+1][256]
     DevBuf<BlockInfo> d_blocks;
@@ -123,6 +124,7 @@ int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, doub
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
 int single_setup(Sector& s);
 int build_descriptors(Sector& s);
+int set_launch(Sector& s, int minb, int ctas_per_sm);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,

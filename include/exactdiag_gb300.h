@@ -51,6 +51,13 @@ int ed_sector_destroy(ed_sector* s);
  * calc_basis_map (general/basis_indexing.h:188-261). Synchronises `stream`. */
 int ed_basis_build(ed_sector* s, void* stream);
 
+/* Launch configuration of the fused Lanczos step (tuning; no reference counterpart):
+ * min_ctas_per_sm selects the compiled variant (3 or 4 resident CTAs per SM, i.e. a register
+ * budget of 85 or 64 per thread) and ctas_per_sm the persistent grid (0 = as many as fit).
+ * exactdiag_gb300.autotune times the candidates and caches the fastest per sector shape. */
+int ed_sector_set_launch(ed_sector* s, int min_ctas_per_sm, int ctas_per_sm);
+int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
+
 /* Number of representatives (Basis_Index_Map::get_num_states, basis_indexing.h:180-182). */
 int ed_basis_size(const ed_sector* s, int64_t* n);
 

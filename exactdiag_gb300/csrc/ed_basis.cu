@@ -282,6 +282,12 @@ __global__ void fill_rows_kernel(SectorView S, int64_t spin_words, uint64_t n_sp
     }
 }
 
+__global__ void interleave_bitmap_kernel(int64_t words, const uint64_t* __restrict__ bitmap,
+                                         const int64_t* __restrict__ prefix, ulonglong2* __restrict__ out) {
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
+        out[w] = make_ulonglong2(bitmap[w], (unsigned long long)prefix[w]);
+}
+
 __global__ void export_sparse_kernel(SectorView S, uint64_t n_spin, int64_t* __restrict__ sparse,
                                      int32_t* __restrict__ orbit_out) {
     extern __shared__ uint32_t s_tab[];
@@ -385,7 +391,16 @@ int basis_build(Sector& s, cudaStream_t st) {
                                                                                      s.d_prefix.p, s.d_keys.p,
                                                                                      s.d_orbit.p);
     ED_CHECK_LAUNCH("fill_rows_kernel");
+    if (!s.d_bitpref.alloc(total_words)) return set_error(ED_ERR_NOMEM, "basis: allocating the bitmap index");
+    interleave_bitmap_kernel<<<grid_for(total_words, 256, s.num_sms), 256, 0, st>>>(total_words, s.d_bitmap.p,
+                                                                                     s.d_prefix.p, s.d_bitpref.p);
+    ED_CHECK_LAUNCH("interleave_bitmap_kernel");
     if (cudaStreamSynchronize(st) != cudaSuccess) return set_error(ED_ERR_CUDA, "basis: fill rows");
+    V.bitpref = s.d_bitpref.p;
+    s.d_bitmap.reset();
+    s.d_prefix.reset();
+    V.bitmap = nullptr;
+    V.word_prefix = nullptr;
     (void)N;
     s.built = true;
     return ED_OK;

@@ -21,7 +21,7 @@ namespace ed {
 
 // Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
 // (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
-constexpr int kChunkRows = 2048;
+constexpr int kChunkRows = 4096;
 
 __device__ __forceinline__ void chunk_reduce(double v[kReduceSlots], double* __restrict__ out) {
     __shared__ double red[kReduceSlots][32];
@@ -96,20 +96,51 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
     }
 }
 
-// One CTA per sector: a_k, b_{k+1} from the sector's chunk partials (fixed order).
-__global__ void lanczos_scalars_kernel(const double* __restrict__ partials, const int* __restrict__ cfirst,
-                                      const int* __restrict__ ccount, double* __restrict__ scal, int stride, int k,
-                                      int norm_mode, int norm_off) {
+// One CTA of kScalarThreads per sector: a_k, b_{k+1} from the sector's chunk partials.  Each thread
+// sums a fixed strided subset of chunks in four independent partial sums (loads stay in flight);
+// the order depends only on the chunk count, so every launch configuration gives the same bits.
+constexpr int kScalarThreads = 512;
+
+__global__ void __launch_bounds__(kScalarThreads)
+    lanczos_scalars_kernel(const double* __restrict__ partials, const int* __restrict__ cfirst,
+                           const int* __restrict__ ccount, double* __restrict__ scal, int stride, int k,
+                           int norm_mode, int norm_off) {
     __shared__ double red[kReduceSlots][32];
     const int s = blockIdx.x;
-    double t[kReduceSlots] = {0.0, 0.0, 0.0, 0.0};
-    for (int c = threadIdx.x; c < ccount[s]; c += blockDim.x)
+    const int cnt = ccount[s];
+    const double2* P = reinterpret_cast<const double2*>(partials + (int64_t)cfirst[s] * kReduceSlots);
+    double t[4][kReduceSlots] = {};
+    int c = threadIdx.x;
+    for (; c + 3 * kScalarThreads < cnt; c += 4 * kScalarThreads) {
+        double2 q[4][2];
 #pragma unroll
-        for (int q = 0; q < kReduceSlots; ++q) t[q] += partials[(int64_t)(cfirst[s] + c) * kReduceSlots + q];
+        for (int u = 0; u < 4; ++u) {
+            q[u][0] = P[2 * (c + u * kScalarThreads)];
+            q[u][1] = P[2 * (c + u * kScalarThreads) + 1];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            t[u][0] += q[u][0].x;
+            t[u][1] += q[u][0].y;
+            t[u][2] += q[u][1].x;
+            t[u][3] += q[u][1].y;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        const int cc = c + u * kScalarThreads;
+        if (cc < cnt) {
+            const double2 q0 = P[2 * cc], q1 = P[2 * cc + 1];
+            t[u][0] += q0.x;
+            t[u][1] += q0.y;
+            t[u][2] += q1.x;
+            t[u][3] += q1.y;
+        }
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int q = 0; q < kReduceSlots; ++q) {
-        double v = t[q];
+        double v = (t[0][q] + t[1][q]) + (t[2][q] + t[3][q]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) red[q][wid] = v;
@@ -151,30 +182,69 @@ __global__ void norm_partials_kernel(const int64_t* __restrict__ offs, const Bat
     }
 }
 
-// mode 0: v_next = (y - a v) / b (step update); mode 1: v *= 1/|v0| (start vector)
+// mode 0: v_next = (y - a v) / b (step update); mode 1: v *= 1/|v0| (start vector).
+// Every real component (the real and imaginary parts alike) is updated the same way, so a chunk
+// whose rows start on a 16-byte boundary is moved as 16-byte vectors, all of a thread's loads
+// issued before its stores; the ragged tail of the last chunk goes row by row.
+constexpr int kUpdThreads = 256;
+
 template <typename R, bool CPLX>
-__global__ void lanczos_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
-                                     int nchunks, void* v, void* other, const double* __restrict__ scal, int stride,
-                                     int k, int mode, int norm_off) {
+__global__ void __launch_bounds__(kUpdThreads)
+    lanczos_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks, int nchunks,
+                          void* v, void* other, const double* __restrict__ scal, int stride, int k, int mode,
+                          int norm_off) {
+    using T = typename Vec<R, CPLX>::T;
+    constexpr int kComp = 16 / sizeof(R);                   // real components per 16-byte vector
+    constexpr int kRowsPerVec = 16 / sizeof(T);             // rows per 16-byte vector
+    constexpr int kIt = kChunkRows / kRowsPerVec / kUpdThreads;  // vectors per thread in a full chunk
+    static_assert(kChunkRows % (kRowsPerVec * kUpdThreads) == 0, "chunk must split into whole vectors");
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
         const double* X = scal + (int64_t)ch.sec * stride;
-        void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
+        T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(v, offs[ch.sec])) + ch.begin;
+        T* y = mode == 1 ? x : reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
+        R a, inv;
         if (mode == 1) {
             const double nv = X[norm_off];
-            const R inv = nv > 0.0 ? (R)(1.0 / nv) : R(0);
-            for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
-                R xr, xi;
-                ld<R, CPLX>(x, i, xr, xi);
-                st<R, CPLX>(x, i, xr * inv, xi * inv);
-            }
-            continue;
+            a = R(0);
+            inv = nv > 0.0 ? (R)(1.0 / nv) : R(0);
+        } else {
+            a = (R)X[2 * k + 1];
+            inv = X[2 * k + 3] != 0.0 ? R(1) : (R)(1.0 / X[2 * k + 2]);
         }
-        void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
-        const R a = (R)X[2 * k + 1];
-        const bool brk = X[2 * k + 3] != 0.0;
-        const R inv = brk ? R(1) : (R)(1.0 / X[2 * k + 2]);
-        for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
+        const int rows = (int)(ch.end - ch.begin);
+        int done = 0;
+        if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15u) == 0) {
+            const int nvec = rows / kRowsPerVec;
+            const uint4* xs = reinterpret_cast<const uint4*>(x);
+            uint4* ys = reinterpret_cast<uint4*>(y);
+            constexpr int kBatch = kIt < 4 ? kIt : 4;  // 16-byte vectors per array in flight per thread
+#pragma unroll 1
+            for (int u0 = 0; u0 < kIt; u0 += kBatch) {
+                uint4 xa[kBatch], ya[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const int q = threadIdx.x + (u0 + u) * kUpdThreads;
+                    if (q < nvec) {
+                        xa[u] = __ldcs(xs + q);
+                        ya[u] = mode == 1 ? xa[u] : __ldcs(ys + q);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const int q = threadIdx.x + (u0 + u) * kUpdThreads;
+                    if (q < nvec) {
+                        const R* xv = reinterpret_cast<const R*>(&xa[u]);
+                        R* yv = reinterpret_cast<R*>(&ya[u]);
+#pragma unroll
+                        for (int e = 0; e < kComp; ++e) yv[e] = (yv[e] - a * xv[e]) * inv;
+                        __stcs(ys + q, ya[u]);
+                    }
+                }
+            }
+            done = nvec * kRowsPerVec;
+        }
+        for (int i = done + threadIdx.x; i < rows; i += kUpdThreads) {
             R vr, vi, yr, yi;
             ld<R, CPLX>(x, i, vr, vi);
             ld<R, CPLX>(y, i, yr, yi);
@@ -237,8 +307,8 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // start vectors: |v0| and normalisation
     norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
-    lanczos_scalars_kernel<<<nsec, 256, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1, stride - 1);
-    lanczos_update_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
+    lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1, stride - 1);
+    lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
                                                         1, stride - 1);
     ED_CHECK_LAUNCH("batch start vectors");
     cudaStream_t cap = st;
@@ -258,8 +328,8 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         void* other = b[(k + 1) % 2];
         lanczos_hv_kernel<R, CPLX, 3><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
                                                                     other, k == 0, coef, stride, k, partials.p);
-        lanczos_scalars_kernel<<<nsec, 256, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
-        lanczos_update_kernel<R, CPLX><<<grid, 256, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0,
+        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
+        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0,
                                                              0);
     }
     if (use_graph) {
@@ -350,7 +420,7 @@ static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, c
     const int rc = (s.hv_minb == 4) ? single_hv_variant<R, CPLX, 4>(s, w, v, vprev, vnext, scal, st)
                                     : single_hv_variant<R, CPLX, 3>(s, w, v, vprev, vnext, scal, st);
     if (rc != ED_OK) return rc;
-    lanczos_scalars_kernel<<<1, 256, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
+    lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
     ED_CHECK_LAUNCH("lanczos_scalars_kernel");
     return ED_OK;
 }
@@ -397,7 +467,7 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
 
 template <typename R, bool CPLX>
 static void single_update_typed(const Sector& s, const void* v, void* vnext, const double* scal, cudaStream_t st) {
-    lanczos_update_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks,
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks,
                                                                  const_cast<void*>(v), vnext, scal, 0, 0, 0, 0);
 }
 
@@ -425,8 +495,8 @@ template <typename R, bool CPLX>
 static void single_norm_typed(const Sector& s, void* x, double* norm, cudaStream_t st) {
     norm_partials_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x,
                                                                 s.d_partials.p);
-    lanczos_scalars_kernel<<<1, 256, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, norm, 0, 0, 1, 0);
-    lanczos_update_kernel<R, CPLX><<<step_grid(s), 256, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x, nullptr,
+    lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, norm, 0, 0, 1, 0);
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x, nullptr,
                                                                  norm, 0, 0, 1, 0);
 }
 

@@ -17,6 +17,7 @@
 // as its exponent e mod 2L, which makes the reference's |amp - 1| > 1e-8 tests
 // (symmetry_ladder.h:196-224) exact integer tests.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -66,36 +67,46 @@ struct CandParams {
     uint8_t pad;
 };
 
-struct HopDesc {
-    uint8_t term;    // 0 tl (leg), 1 tr (rung)
-    uint8_t a, b;    // electron site, hole site
+// A hop of the fast row.  The first 32 bytes are what the row kernel reads for every row (as two
+// 16-byte words in hv_row_fast); keep their order.
+struct alignas(16) HopDesc {
+    uint32_t band;   // compressed bits that shift by one position
+    uint32_t swap;   // cand[0].swap
     uint8_t p, q;    // electron's compressed position before (row mask) and after (new mask) the hop
-    int8_t sign;     // fermion sign (electrons strictly between a and b)
+    uint8_t rot, e;  // cand[0].rot, cand[0].e
+    uint8_t term;    // 0 tl (leg), 1 tr (rung)
     uint8_t mode;    // kModeFree / kModeCand / kModeGeneric / kModeAbsent
     uint8_t ncand;
-    uint32_t keep;   // compressed bits the move leaves in place
-    uint32_t band;   // compressed bits that shift by one position
-    int32_t block;   // target block
-    uint32_t pad;
+    int8_t sign;     // fermion sign (electrons strictly between a and b)
     int64_t start, word_off;  // target block rows and bitmap
+    // read by the candidate and generic modes only
+    uint8_t a, b;    // electron site, hole site
+    uint8_t pad[2];
+    int32_t block;   // target block
     CandParams cand[kMaxCand];
 };
 
-struct BlockDesc {
+// Descriptor of one block.  The first 32 bytes are read per row as two 16-byte words; keep
+// their order.
+struct alignas(16) BlockDesc {
     uint32_t hmask;
+    uint32_t m_rung;     // rung bonds, at the lower compressed position (partner one above)
+    uint32_t m_legadj;   // leg bonds whose middle site is a hole (partner one above)
+    uint32_t m_legd2;    // leg bonds whose middle site is occupied (partner two above)
     uint8_t mode;        // kModeFree / kModeCand / kModeGeneric
     uint8_t nhop;
     uint8_t ncand;
     uint8_t nwrap;
-    int64_t start, word_off;
-    uint32_t m_rung;     // rung bonds, at the lower compressed position (partner one above)
-    uint32_t m_legadj;   // leg bonds whose middle site is a hole (partner one above)
-    uint32_t m_legd2;    // leg bonds whose middle site is occupied (partner two above)
     uint8_t wrap[2][2];  // leg bonds across the periodic boundary: compressed positions (lo, hi)
-    uint8_t pad[4];
+    int64_t start;
+    int64_t word_off;
+    uint8_t pad[8];
     CandParams cand[kMaxCand];  // stabiliser of hmask (exchange targets in kModeCand blocks)
     HopDesc hop[kMaxHops];
 };
+
+static_assert(offsetof(HopDesc, start) == 16 && offsetof(HopDesc, a) == 32, "HopDesc hot words");
+static_assert(offsetof(BlockDesc, mode) == 16 && offsetof(BlockDesc, start) == 24, "BlockDesc hot words");
 
 // Read-only view of a built sector, passed to kernels by value.
 struct SectorView {
@@ -111,8 +122,9 @@ struct SectorView {
     const HoleEntry* holes;        // may be null: generic mode (block found by binary search)
     const uint64_t* keys;          // [n] packed representative keys, ascending
     const uint8_t* orbit;          // [n] orbit size (num_sparse_states_in_dense)
-    const uint64_t* bitmap;        // candidate bitmaps of non-free blocks
-    const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word
+    const uint64_t* bitmap;        // candidate bitmaps of every block (basis construction only)
+    const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word (construction only)
+    const ulonglong2* bitpref;     // {bitmap word, its prefix} side by side: one 16-byte load per lookup
     const uint32_t* rank_tab;      // byte tables of the colex spin rank (compact layout, see RankTab)
     uint32_t rk_off[4];            // first word of byte-chunk c's table
     uint32_t rk_sh[4];             // log2 of the entries per k of chunk c (8, or fewer for the top chunk)

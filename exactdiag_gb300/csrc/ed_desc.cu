@@ -154,7 +154,6 @@ int build_descriptors(Sector& s) {
                 else
                     for (int c = H.q; c < H.p; ++c) band |= 1u << c;
                 H.band = band;
-                H.keep = ~(band | (1u << H.p));
                 const HoleEntry he = holes[hole_rank(h2, &comb[0][0])];
                 H.block = he.block;
                 if (he.block < 0) {
@@ -166,6 +165,9 @@ int build_descriptors(Sector& s) {
                     const int nc = coset(S, h2, T.hmask, H.cand);
                     H.ncand = (uint8_t)std::min(nc, kMaxCand);
                     H.mode = (nc == 1) ? kModeFree : (nc <= kMaxCand ? kModeCand : kModeGeneric);
+                    H.swap = H.cand[0].swap;
+                    H.rot = H.cand[0].rot;
+                    H.e = H.cand[0].e;
                 }
                 if (nh < kMaxHops) D.hop[nh++] = H;
             }

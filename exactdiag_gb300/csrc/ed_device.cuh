@@ -97,11 +97,10 @@ __device__ __forceinline__ int64_t dense_in_block(const SectorView& S, const Blo
                                                   const RankTab& rank_tab) {
     const uint32_t r = spin_rank(compress_spins(dr, B.hmask), rank_tab, S.Nd);
     if (B.flags & kBlockFree) return B.start + (int64_t)r;
-    const int64_t w = B.word_off + (r >> 6);
-    const uint64_t bits = S.bitmap[w];
+    const ulonglong2 bp = S.bitpref[B.word_off + (r >> 6)];
     const uint64_t bit = 1ull << (r & 63u);
-    if (!(bits & bit)) return -1;
-    return S.word_prefix[w] + __popcll(bits & (bit - 1ull));
+    if (!(bp.x & bit)) return -1;
+    return (int64_t)bp.y + __popcll(bp.x & (bit - 1ull));
 }
 
 struct Resolved {
@@ -255,10 +254,11 @@ __device__ __forceinline__ void hv_row(const SectorView& S, const HvTables<R>& t
 
 // ------------------------------------------------------------------ fast row (descriptors)
 
+// Left rotation of an Ns-bit mask (0 <= r < Ns, 1 <= Ns <= 32): bits pushed above Ns by the
+// left shift are the ones the right shift brings back in at the bottom, so both run in 32 bits.
 __device__ __forceinline__ uint32_t rot_ns(uint32_t x, int r, int Ns) {
-    const uint64_t m = (Ns == 32) ? 0xffffffffull : ((1ull << Ns) - 1ull);
-    const uint64_t xx = x;
-    return (uint32_t)(((xx << r) | (xx >> (Ns - r))) & m);
+    const uint32_t m = 0xffffffffu >> (32 - Ns);
+    return ((x << r) | (x >> ((Ns - r) & 31))) & m;
 }
 
 __device__ __forceinline__ uint32_t swap_pairs(uint32_t x, uint32_t m) {
@@ -295,11 +295,10 @@ __device__ __forceinline__ CandResult resolve_cand(const CandParams* c, int nc, 
 }
 
 __device__ __forceinline__ int64_t bitmap_row(const SectorView& S, int64_t word_off, uint32_t r) {
-    const int64_t w = word_off + (r >> 6);
-    const uint64_t bits = S.bitmap[w];
+    const ulonglong2 bp = S.bitpref[word_off + (r >> 6)];
     const uint64_t bit = 1ull << (r & 63u);
-    if (!(bits & bit)) return -1;
-    return S.word_prefix[w] + __popcll(bits & (bit - 1ull));
+    if (!(bp.x & bit)) return -1;
+    return (int64_t)bp.y + __popcll(bp.x & (bit - 1ull));
 }
 
 template <typename R, bool CPLX>
@@ -369,16 +368,24 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
     const int Ns = S.Ns, N = S.N;
     ld<R, CPLX>(x, i, xir, xii);
     const uint32_t dc = compress_spins(d, h);
-    const bool row_free = (D->mode == kModeFree);
+    // hot words of the descriptor: {hmask, m_rung, m_legadj, m_legd2}, {mode|nhop|ncand|nwrap, wrap, start}
+    const uint4 dw0 = reinterpret_cast<const uint4*>(D)[0];
+    const uint4 dw1 = reinterpret_cast<const uint4*>(D)[1];
+    const bool row_free = (dw1.x & 255u) == kModeFree;
+    const int nhop = (dw1.x >> 8) & 255u, nwrap = dw1.x >> 24;
+    const int wlo[2] = {(int)(dw1.y & 255u), (int)((dw1.y >> 16) & 255u)};
+    const int whi[2] = {(int)((dw1.y >> 8) & 255u), (int)(dw1.y >> 24)};
+    const int64_t dstart = (int64_t)(((uint64_t)dw1.w << 32) | dw1.z);
     const int Ni = row_free ? N : (int)S.orbit[i];
     const R sqNi = tb.sqrtv[Ni];
     R accr = R(0), acci = R(0);
     // exchange bonds (jl, jr)
     const uint32_t dif1 = dc ^ (dc >> 1), dif2 = dc ^ (dc >> 2);
-    const uint32_t mr = D->m_rung & dif1, ma = D->m_legadj & dif1, m2 = D->m_legd2 & dif2;
+    const uint32_t mr = dw0.y & dif1, ma = dw0.z & dif1, m2 = dw0.w & dif2;
     uint32_t wrap_anti = 0;
-    const int nwrap = D->nwrap;
-    for (int t = 0; t < nwrap; ++t) wrap_anti |= (((dc >> D->wrap[t][0]) ^ (dc >> D->wrap[t][1])) & 1u) << t;
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+        if (t < nwrap) wrap_anti |= (((dc >> wlo[t]) ^ (dc >> whi[t])) & 1u) << t;
     const R wl = w[2], wr = w[3];
     const R diag = R(-0.5) * (wr * (R)__popc(mr) + wl * (R)(__popc(ma) + __popc(m2) + __popc(wrap_anti)));
     int64_t jj[4];
@@ -388,8 +395,8 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         // every neighbour in the block is a representative with orbit 2L and phase 1: y += w/2 x_j,
         // at row i + delta of the same block (32-bit offsets from the block's first row)
         const R cr = R(0.5) * wr, cl = R(0.5) * wl;
-        const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(x) + D->start;
-        const uint32_t ri = (uint32_t)(i - D->start);
+        const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(x) + dstart;
+        const uint32_t ri = (uint32_t)(i - dstart);
         uint32_t off[4];
         R cb[4];
         uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
@@ -438,7 +445,7 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                 off[u] = ri;
                 cb[u] = R(0);
                 if (u < 2 && ((wrap_anti >> u) & 1u)) {
-                    const uint32_t dc2 = dc ^ (1u << D->wrap[u][0]) ^ (1u << D->wrap[u][1]);
+                    const uint32_t dc2 = dc ^ (1u << wlo[u]) ^ (1u << whi[u]);
                     off[u] = spin_rank(dc2, tb.rank, S.Nd);
                     cb[u] = cl;
                     live |= 1u << u;
@@ -447,33 +454,35 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
             gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
         }
     } else {
-        // non-free block: each exchange target is resolved through the block's stabiliser
+        // non-free block: each exchange target is resolved through the block's stabiliser (lowest
+        // image, orbit, phase agreement), then its bitmap word
+        const int ncand = (dw1.x >> 16) & 255u;
+        const int64_t word_off = D->word_off;
+        const R cr = R(0.5) * wr * sqNi, cl = R(0.5) * wl * sqNi;
 #pragma unroll 1
         for (int kind = 0; kind < 4; ++kind) {
             uint32_t m;
             int dist;
-            R wt;
-            if (kind == 0) { m = mr; dist = 1; wt = wr; }
-            else if (kind == 1) { m = ma; dist = 1; wt = wl; }
-            else if (kind == 2) { m = m2; dist = 2; wt = wl; }
-            else { m = wrap_anti; dist = 0; wt = wl; }
-            if (wt == R(0)) continue;
-            const R coef = R(0.5) * wt * sqNi;
+            R coef;
+            if (kind == 0) { m = mr; dist = 1; coef = cr; }
+            else if (kind == 1) { m = ma; dist = 1; coef = cl; }
+            else if (kind == 2) { m = m2; dist = 2; coef = cl; }
+            else { m = wrap_anti; dist = 0; coef = cl; }
+            if (coef == R(0)) continue;
             while (m) {
                 const int a = __ffs(m) - 1;
                 m &= m - 1u;
                 const uint32_t flip = dist ? ((1u << a) | (1u << (a + dist)))
-                                           : ((1u << D->wrap[a][0]) | (1u << D->wrap[a][1]));
-                const CandResult cr2 = resolve_cand(D->cand, D->ncand, dc ^ flip, Ns);
+                                           : ((1u << (a ? wlo[1] : wlo[0])) | (1u << (a ? whi[1] : whi[0])));
+                const CandResult cr2 = resolve_cand(D->cand, ncand, dc ^ flip, Ns);
                 if (!cr2.valid) continue;
-                const int64_t j = bitmap_row(S, D->word_off, spin_rank(cr2.best, tb.rank, S.Nd));
+                const int64_t j = bitmap_row(S, word_off, spin_rank(cr2.best, tb.rank, S.Nd));
                 if (j < 0) continue;
                 gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N / cr2.count], cr2.e, tb, accr, acci);
             }
         }
     }
     // hops (tl, tr), four at a time
-    const int nhop = D->nhop;
 #pragma unroll 1
     for (int t0 = 0; t0 < nhop; t0 += 4) {
 #pragma unroll
@@ -484,26 +493,33 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
             const int t = t0 + u;
             if (t >= nhop) continue;
             const HopDesc& H = D->hop[t];
-            const R wt = H.term ? w[1] : w[0];
-            if (wt == R(0) || H.mode == kModeAbsent) continue;
-            const R coef = (H.sign > 0 ? -wt : wt) * sqNi;
-            if (H.mode == kModeGeneric) {
+            // hot words: {band, swap, p|q|rot|e, term|mode|ncand|sign}, {start, word_off}
+            const uint4 hw = reinterpret_cast<const uint4*>(&H)[0];
+            const uint32_t hmode = (hw.w >> 8) & 255u;
+            const R wt = (hw.w & 255u) ? w[1] : w[0];
+            if (wt == R(0) || hmode == kModeAbsent) continue;
+            const R coef = ((hw.w >> 24) == 1u ? -wt : wt) * sqNi;
+            if (hmode == kModeGeneric) {
                 const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
                 const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
                 add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
                 continue;
             }
-            const uint32_t moved = (H.q > H.p) ? ((dc & H.band) >> 1) : ((dc & H.band) << 1);
-            const uint32_t dcm = (dc & H.keep) | moved | (((dc >> H.p) & 1u) << H.q);
-            if (H.mode == kModeFree) {
-                const uint32_t dct = cand_image(H.cand[0], dcm, Ns);
-                jj[u] = H.start + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+            const uint4 hw1 = reinterpret_cast<const uint4*>(&H)[1];
+            const int p = hw.z & 255u, q = (hw.z >> 8) & 255u;
+            const uint32_t band = hw.x;
+            const uint32_t moved = (q > p) ? ((dc & band) >> 1) : ((dc & band) << 1);
+            const uint32_t dcm = (dc & ~(band | (1u << p))) | moved | (((dc >> p) & 1u) << q);
+            if (hmode == kModeFree) {
+                const uint32_t dct = rot_ns(swap_pairs(dcm, hw.y), (hw.z >> 16) & 255u, Ns);
+                jj[u] = (int64_t)(((uint64_t)hw1.y << 32) | hw1.x) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
                 cc[u] = coef * tb.rsqrtv[N];
-                ee[u] = H.cand[0].e;
+                ee[u] = hw.z >> 24;
             } else {
-                const CandResult cr2 = resolve_cand(H.cand, H.ncand, dcm, Ns);
+                const CandResult cr2 = resolve_cand(H.cand, (hw.w >> 16) & 255u, dcm, Ns);
                 if (!cr2.valid) continue;
-                const int64_t j = bitmap_row(S, H.word_off, spin_rank(cr2.best, tb.rank, S.Nd));
+                const int64_t j =
+                    bitmap_row(S, (int64_t)(((uint64_t)hw1.w << 32) | hw1.z), spin_rank(cr2.best, tb.rank, S.Nd));
                 if (j < 0) continue;
                 jj[u] = j;
                 cc[u] = coef * tb.rsqrtv[N / cr2.count];

@@ -82,6 +82,7 @@ struct Sector {
     DevBuf<HoleEntry> d_holes;
     DevBuf<uint64_t> d_bitmap;
     DevBuf<int64_t> d_prefix;
+    DevBuf<ulonglong2> d_bitpref;
     DevBuf<uint64_t> d_keys;
     DevBuf<uint8_t> d_orbit;
     DevBuf<double> d_partials;   // [hv_grid][kReduceSlots] scratch of the fused Lanczos step

@@ -15,86 +15,9 @@
 #include <mutex>
 #include <vector>
 
-#include "ed_device.cuh"
+#include "ed_step.cuh"
 
 namespace ed {
-
-// Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
-// (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
-constexpr int kChunkRows = 4096;
-
-__device__ __forceinline__ void chunk_reduce(double v[kReduceSlots], double* __restrict__ out) {
-    __shared__ double red[kReduceSlots][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < kReduceSlots; ++k) {
-        double t = v[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) red[k][wid] = t;
-    }
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int k = 0; k < kReduceSlots; ++k) {
-            double t = lane < nw ? red[k][lane] : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-            if (lane == 0) out[k] = t;
-        }
-    }
-    __syncthreads();
-}
-
-template <typename R, bool CPLX>
-__device__ __forceinline__ void* vec_at(void* base, int64_t off) {
-    return reinterpret_cast<typename Vec<R, CPLX>::T*>(base) + off;
-}
-
-template <typename R, bool CPLX, int MINB>
-__global__ void __launch_bounds__(kHvThreads, MINB)
-    lanczos_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
-                    const BatchChunk* __restrict__ chunks, int nchunks, HvWeights W, void* v, void* vprev, void* other,
-                    int first, const double* __restrict__ scal, int stride, int k, double* __restrict__ partials) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    const HvTables<R> tb = load_tables<R>(views[0], smem);
-    const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
-    __shared__ __align__(16) BlockDesc sdesc;
-    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const BatchChunk ch = chunks[c];
-        const SectorView S = views[ch.sec];
-        const BlockDesc* staged = W.faithful ? nullptr : stage_desc(S, tb.comb, ch.begin, &sdesc);
-        const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
-        void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
-        const void* yp = first ? nullptr : vec_at<R, CPLX>(vprev, offs[ch.sec]);
-        const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
-        Accum<R> acc[kReduceSlots];
-        for (int64_t i = ch.begin + threadIdx.x; i < ch.end; i += blockDim.x) {
-            R hr, hi, xr, xi;
-            hv_row_any<R, CPLX>(S, tb, w, W.faithful, i, x, hr, hi, xr, xi, staged);
-            R yr = hr, yi = hi;
-            if (!first) {
-                R pr, pi;
-                ld<R, CPLX>(yp, i, pr, pi);  // v_{k-1}; may be the same buffer as y (read before written)
-                yr -= beta * pr;
-                if constexpr (CPLX) yi -= beta * pi;
-            }
-            st<R, CPLX>(y, i, yr, yi);
-            acc[0].add_prod(xr, hr);
-            acc[1].add_prod(yr, yr);
-            acc[2].add_prod(xr, yr);
-            acc[3].add_prod(xr, xr);
-            if constexpr (CPLX) {
-                acc[0].add_prod(xi, hi);
-                acc[1].add_prod(yi, yi);
-                acc[2].add_prod(xi, yi);
-                acc[3].add_prod(xi, xi);
-            }
-        }
-        double tot[kReduceSlots] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
-        chunk_reduce(tot, partials + (int64_t)c * kReduceSlots);
-    }
-}
 
 // One CTA of kScalarThreads per sector: a_k, b_{k+1} from the sector's chunk partials.  Each thread
 // sums a fixed strided subset of chunks in four independent partial sums (loads stay in flight);
@@ -204,20 +127,38 @@ __global__ void __launch_bounds__(kUpdThreads)
         T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(v, offs[ch.sec])) + ch.begin;
         T* y = mode == 1 ? x : reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
         R a, inv;
+        // FP32 vectors take the reciprocal in FP32 (the FP64 units are slow on this part)
+        auto recip = [](double b) -> R {
+            if constexpr (sizeof(R) == 4) return __frcp_rn((float)b);
+            else return 1.0 / b;
+        };
         if (mode == 1) {
             const double nv = X[norm_off];
             a = R(0);
-            inv = nv > 0.0 ? (R)(1.0 / nv) : R(0);
+            inv = nv > 0.0 ? recip(nv) : R(0);
         } else {
             a = (R)X[2 * k + 1];
-            inv = X[2 * k + 3] != 0.0 ? R(1) : (R)(1.0 / X[2 * k + 2]);
+            inv = X[2 * k + 3] != 0.0 ? R(1) : recip(X[2 * k + 2]);
         }
         const int rows = (int)(ch.end - ch.begin);
-        int done = 0;
-        if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15u) == 0) {
-            const int nvec = rows / kRowsPerVec;
-            const uint4* xs = reinterpret_cast<const uint4*>(x);
-            uint4* ys = reinterpret_cast<uint4*>(y);
+        // rows before the first 16-byte boundary (chunks start where blocks start) go row by row
+        const uintptr_t ax = reinterpret_cast<uintptr_t>(x), ay = reinterpret_cast<uintptr_t>(y);
+        int head = rows;
+        if (((ax ^ ay) & 15u) == 0 && (ax % sizeof(T)) == 0) {
+            head = (int)(((16u - (ax & 15u)) & 15u) / sizeof(T));
+            if (head > rows) head = rows;
+        }
+        for (int i = threadIdx.x; i < head; i += kUpdThreads) {
+            R vr, vi, yr, yi;
+            ld<R, CPLX>(x, i, vr, vi);
+            ld<R, CPLX>(y, i, yr, yi);
+            st<R, CPLX>(y, i, (yr - a * vr) * inv, (yi - a * vi) * inv);
+        }
+        int done = head;
+        if (head < rows) {
+            const int nvec = (rows - head) / kRowsPerVec;
+            const uint4* xs = reinterpret_cast<const uint4*>(x + head);
+            uint4* ys = reinterpret_cast<uint4*>(y + head);
             constexpr int kBatch = kIt < 4 ? kIt : 4;  // 16-byte vectors per array in flight per thread
 #pragma unroll 1
             for (int u0 = 0; u0 < kIt; u0 += kBatch) {
@@ -242,7 +183,7 @@ __global__ void __launch_bounds__(kUpdThreads)
                     }
                 }
             }
-            done = nvec * kRowsPerVec;
+            done = head + nvec * kRowsPerVec;
         }
         for (int i = done + threadIdx.x; i < rows; i += kUpdThreads) {
             R vr, vi, yr, yi;
@@ -253,16 +194,62 @@ __global__ void __launch_bounds__(kUpdThreads)
     }
 }
 
-// Chunk table of one sector (rows [0, n) cut every kChunkRows), appended to `out`.
-static void append_chunks(int sec, int64_t n, std::vector<BatchChunk>& out) {
-    for (int64_t b = 0; b < n; b += kChunkRows) {
-        BatchChunk c{};
-        c.sec = sec;
-        c.begin = b;
-        c.end = std::min<int64_t>(n, b + kChunkRows);
-        out.push_back(c);
+// Chunks of every sector: each block's rows cut every kChunkRows (a chunk never straddles two
+// blocks), sector-major in row order; the chunk ids grouped by row kind.
+void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
+    const int nsec = (int)secs.size();
+    P.chunks.clear();
+    P.kind_idx.clear();
+    P.cfirst.assign(nsec, 0);
+    P.ccount.assign(nsec, 0);
+    std::vector<int> by_kind[4];
+    for (int s = 0; s < nsec; ++s) {
+        const Sector& S = *secs[s];
+        P.cfirst[s] = (int)P.chunks.size();
+        auto add_span = [&](int64_t start, int64_t count, int block, int kind) {
+            for (int64_t b = 0; b < count; b += kChunkRows) {
+                BatchChunk c{};
+                c.sec = s;
+                c.block = block;
+                c.begin = start + b;
+                c.end = start + std::min<int64_t>(count, b + kChunkRows);
+                by_kind[kind].push_back((int)P.chunks.size());
+                P.chunks.push_back(c);
+            }
+        };
+        if (S.spans.empty()) add_span(0, S.view.n, -1, kRowsGeneric);
+        for (const BlockSpan& sp : S.spans)
+            if (sp.count > 0) add_span(sp.start, sp.count, sp.block, sp.kind);
+        P.ccount[s] = (int)P.chunks.size() - P.cfirst[s];
+    }
+    for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind) {
+        P.kind_first[kind] = (int)P.kind_idx.size();
+        P.kind_count[kind] = (int)by_kind[kind].size();
+        P.kind_idx.insert(P.kind_idx.end(), by_kind[kind].begin(), by_kind[kind].end());
     }
 }
+
+// The fused H.v pass of one step over every row kind of a plan (device tables in `a`, whose idx
+// points at the whole kind-ordered id list), one launch per kind present.
+static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, const int kind_first[4],
+                       const int kind_count[4], StepArgs a, cudaStream_t st) {
+    const int* idx0 = a.idx;
+    a.idx = idx0 + kind_first[kRowsFree];
+    a.count = kind_count[kRowsFree];
+    a.grid = free_grid;
+    if (int rc = step_hv_free(dtype, minb, a, st)) return rc;
+    a.idx = idx0 + kind_first[kRowsCand];
+    a.count = kind_count[kRowsCand];
+    a.grid = other_grid;
+    if (int rc = step_hv_cand(dtype, a, st)) return rc;
+    a.idx = idx0 + kind_first[kRowsGeneric];
+    a.count = kind_count[kRowsGeneric];
+    return step_hv_generic(dtype, a, st);
+}
+
+static int dtype_code(bool dbl, bool cplx) { return dbl ? (cplx ? ED_C128 : ED_F64) : (cplx ? ED_C64 : ED_F32); }
+
+static int update_grid(const Sector& s, int nchunks) { return std::max(1, std::min(nchunks, s.num_sms * 8)); }
 
 template <typename R, bool CPLX>
 static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& w, const void* const* v0, int m,
@@ -271,45 +258,45 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     const size_t esz = sizeof(typename Vec<R, CPLX>::T);
     std::vector<SectorView> hviews(nsec);
     std::vector<int64_t> hoffs(nsec);
-    std::vector<BatchChunk> hchunks;
-    std::vector<int> cfirst(nsec), ccount(nsec);
+    ChunkPlan plan;
+    plan_chunks(secs, plan);
     int64_t total = 0;
     for (int s = 0; s < nsec; ++s) {
         hviews[s] = secs[s]->view;
         hoffs[s] = total;
-        cfirst[s] = (int)hchunks.size();
-        append_chunks(s, hviews[s].n, hchunks);
-        ccount[s] = (int)hchunks.size() - cfirst[s];
         total += hviews[s].n;
     }
-    const int nchunks = (int)hchunks.size();
+    const int nchunks = (int)plan.chunks.size();
     const int stride = 2 * m + 4;
     DevBuf<SectorView> dviews(nsec);
     DevBuf<int64_t> doffs(nsec);
     DevBuf<BatchChunk> dchunks(nchunks);
+    DevBuf<int> dkidx(nchunks);
     DevBuf<int> dcfirst(nsec), dccount(nsec);
     DevBuf<double> partials((int64_t)nchunks * kReduceSlots);
     DevBuf<uint8_t> buf0((int64_t)(total * esz)), buf1((int64_t)(total * esz));
-    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dcfirst.ok() || !dccount.ok() || !partials.ok() ||
-        !buf0.ok() || !buf1.ok())
+    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dkidx.ok() || !dcfirst.ok() || !dccount.ok() ||
+        !partials.ok() || !buf0.ok() || !buf1.ok())
         return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
     cudaMemcpyAsync(dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doffs.p, hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dchunks.p, hchunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dcfirst.p, cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dccount.p, ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dchunks.p, plan.chunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dkidx.p, plan.kind_idx.data(), nchunks * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dcfirst.p, plan.cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dccount.p, plan.ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(coef, 0, (size_t)nsec * stride * sizeof(double), st);
     for (int s = 0; s < nsec; ++s)
         if (hviews[s].n)
             cudaMemcpyAsync(buf0.p + hoffs[s] * esz, v0[s], hviews[s].n * esz, cudaMemcpyDeviceToDevice, st);
-    const int grid = std::min(nchunks, secs[0]->hv_grid > 0 ? secs[0]->hv_grid : secs[0]->num_sms * 3);
+    const Sector& s0 = *secs[0];
+    const int grid = update_grid(s0, nchunks);
     const size_t smem = hv_smem_bytes(hviews[0], sizeof(R));
-    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // start vectors: |v0| and normalisation
     norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
-    lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1, stride - 1);
-    lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef, stride, 0,
-                                                        1, stride - 1);
+    lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1,
+                                                           stride - 1);
+    lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef,
+                                                                 stride, 0, 1, stride - 1);
     ED_CHECK_LAUNCH("batch start vectors");
     cudaStream_t cap = st;
     cudaStream_t priv = nullptr;
@@ -326,11 +313,21 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     for (int k = 0; k < m; ++k) {
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
-        lanczos_hv_kernel<R, CPLX, 3><<<grid, kHvThreads, smem, cap>>>(dviews.p, doffs.p, dchunks.p, nchunks, w, v, other,
-                                                                    other, k == 0, coef, stride, k, partials.p);
+        StepArgs a{dviews.p, doffs.p, dchunks.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
+                    partials.p};
+        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid,
+                                 plan.kind_first, plan.kind_count, a, cap)) {
+            if (use_graph) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(cap, &g);
+                if (g) cudaGraphDestroy(g);
+                cudaStreamDestroy(priv);
+            }
+            return rc;
+        }
         lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
-        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef, stride, k, 0,
-                                                             0);
+        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
+                                                                      stride, k, 0, 0);
     }
     if (use_graph) {
         cudaGraph_t graph = nullptr;
@@ -376,21 +373,28 @@ int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights
 // same reduction order), so sequential and batched recursions agree bit for bit.
 
 int single_setup(Sector& s) {
-    std::vector<BatchChunk> ch;
-    append_chunks(0, s.view.n, ch);
+    ChunkPlan plan;
+    plan_chunks({&s}, plan);
     const int64_t zero = 0;
-    const int first = 0, count = (int)ch.size();
+    const int count = (int)plan.chunks.size();
     s.n_chunks = count;
+    for (int kind = 0; kind < 4; ++kind) {
+        s.kind_first[kind] = plan.kind_first[kind];
+        s.kind_count[kind] = plan.kind_count[kind];
+    }
     if (!s.d_self.alloc(1) || !s.d_offs.alloc(1) || !s.d_chunks.alloc(count > 0 ? count : 1) ||
-        !s.d_cfirst.alloc(1) || !s.d_ccount.alloc(1))
+        !s.d_kidx.alloc(count > 0 ? count : 1) || !s.d_cfirst.alloc(1) || !s.d_ccount.alloc(1))
         return set_error(ED_ERR_NOMEM, "sector step tables");
     cudaMemcpy(s.d_self.p, &s.view, sizeof(SectorView), cudaMemcpyHostToDevice);
     cudaMemcpy(s.d_offs.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice);
-    if (count) cudaMemcpy(s.d_chunks.p, ch.data(), count * sizeof(BatchChunk), cudaMemcpyHostToDevice);
-    cudaMemcpy(s.d_cfirst.p, &first, sizeof(int), cudaMemcpyHostToDevice);
-    cudaMemcpy(s.d_ccount.p, &count, sizeof(int), cudaMemcpyHostToDevice);
-    const int64_t slots = (int64_t)std::max(count, s.hv_grid) * kReduceSlots;
-    if (!s.d_partials.alloc(slots)) return set_error(ED_ERR_NOMEM, "sector reduction scratch");
+    if (count) {
+        cudaMemcpy(s.d_chunks.p, plan.chunks.data(), count * sizeof(BatchChunk), cudaMemcpyHostToDevice);
+        cudaMemcpy(s.d_kidx.p, plan.kind_idx.data(), count * sizeof(int), cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy(s.d_cfirst.p, plan.cfirst.data(), sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(s.d_ccount.p, plan.ccount.data(), sizeof(int), cudaMemcpyHostToDevice);
+    if (!s.d_partials.alloc((int64_t)(count > 0 ? count : 1) * kReduceSlots))
+        return set_error(ED_ERR_NOMEM, "sector reduction scratch");
     return ED_OK;
 }
 
@@ -400,56 +404,32 @@ static bool dtype_fits(const Sector& s, int dtype) {
     return false;
 }
 
-static int step_grid(const Sector& s) { return std::max(1, std::min(s.n_chunks, s.hv_grid)); }
-
-template <typename R, bool CPLX, int MINB>
-static int single_hv_variant(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
-                             double* scal, cudaStream_t st) {
-    const size_t smem = hv_smem_bytes(s.view, sizeof(R));
-    cudaFuncSetAttribute(lanczos_hv_kernel<R, CPLX, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    lanczos_hv_kernel<R, CPLX, MINB><<<step_grid(s), kHvThreads, smem, st>>>(
-        s.d_self.p, s.d_offs.p, s.d_chunks.p, s.n_chunks, w, const_cast<void*>(v), const_cast<void*>(vprev), vnext,
-        vprev == nullptr, scal, 0, 0, s.d_partials.p);
-    ED_CHECK_LAUNCH("lanczos_hv_kernel");
-    return ED_OK;
-}
+static int step_grid(const Sector& s) { return update_grid(s, s.n_chunks); }
 
 template <typename R, bool CPLX>
 static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
                            double* scal, cudaStream_t st) {
-    const int rc = (s.hv_minb == 4) ? single_hv_variant<R, CPLX, 4>(s, w, v, vprev, vnext, scal, st)
-                                    : single_hv_variant<R, CPLX, 3>(s, w, v, vprev, vnext, scal, st);
-    if (rc != ED_OK) return rc;
+    StepArgs a{s.d_self.p, s.d_offs.p, s.d_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
+               const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p};
+    if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.hv_grid, s.other_grid, s.kind_first,
+                             s.kind_count, a, st))
+        return rc;
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
     ED_CHECK_LAUNCH("lanczos_scalars_kernel");
     return ED_OK;
 }
 
-// Resident CTAs per SM of the fused step kernel for a sector, per launch variant.
-template <int MINB>
-static int step_occupancy(const SectorView& V) {
-    const size_t smem = hv_smem_bytes(V, sizeof(float));
-    cudaFuncSetAttribute(lanczos_hv_kernel<float, false, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lanczos_hv_kernel<float, false, MINB>, kHvThreads,
-                                                      smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 1;
-    }
-    return per_sm > 0 ? per_sm : 1;
-}
-
+// Launch shape of the step kernels: the free-row kernel's register variant (3 or 4 resident CTAs
+// per SM) and CTAs per SM (0 = as many as fit); the other kinds run as many CTAs as fit.
 int set_launch(Sector& s, int minb, int ctas_per_sm) {
     if (minb != 3 && minb != 4) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: variant must be 3 or 4");
-    const int occ = (minb == 4) ? step_occupancy<4>(s.view) : step_occupancy<3>(s.view);
     if (ctas_per_sm < 0 || ctas_per_sm > 8) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: ctas_per_sm");
+    const size_t smem = hv_smem_bytes(s.view, sizeof(float));
+    const int occ = step_free_occupancy(minb, smem);
     const int per_sm = (ctas_per_sm == 0 || ctas_per_sm > occ) ? occ : ctas_per_sm;
-    const int grid = s.num_sms * per_sm;
-    const int64_t slots = (int64_t)std::max(s.n_chunks, grid) * kReduceSlots;
-    if (s.d_partials.n < slots && !s.d_partials.alloc(slots)) return set_error(ED_ERR_NOMEM, "reduction scratch");
     s.hv_minb = minb;
-    s.hv_grid = grid;
+    s.hv_grid = s.num_sms * per_sm;
+    s.other_grid = s.num_sms * step_rest_occupancy(smem);
     return ED_OK;
 }
 

@@ -86,6 +86,7 @@ int coset(const HostSector& S, uint32_t h, uint32_t hc, CandParams* out) {
 int build_descriptors(Sector& s) {
     SectorView& V = s.view;
     V.desc = nullptr;
+    s.spans.clear();
     if (V.n_blocks == 0 || !V.holes) return ED_OK;
     const HostSector S{V.L, V.N, V.Nh, V.Ns, V.kx, V.ky, V.ne_even, V.mask};
     std::vector<BlockInfo> blocks(V.n_blocks);
@@ -173,8 +174,22 @@ int build_descriptors(Sector& s) {
             }
         }
         D.nhop = (uint8_t)nh;
+        // a block with a hop whose target needs the orbit walk takes the orbit walk for all its rows:
+        // the fast-row kernels then never carry that code
+        for (int t = 0; t < nh; ++t)
+            if (D.hop[t].mode == kModeGeneric) D.mode = kModeGeneric;
         desc[b] = D;
     }
+    // row ranges of the blocks by kind; they tile [0, n) in block order
+    int64_t next = 0;
+    for (int b = 0; b < V.n_blocks; ++b) {
+        const int mode = desc[b].mode;
+        const int kind = mode == kModeFree ? kRowsFree : (mode == kModeCand ? kRowsCand : kRowsGeneric);
+        if (blocks[b].start != next) return set_error(ED_ERR_INTERNAL, "descriptors: block rows are not contiguous");
+        s.spans.push_back(BlockSpan{blocks[b].start, blocks[b].count, b, kind});
+        next += blocks[b].count;
+    }
+    if (next != V.n) return set_error(ED_ERR_INTERNAL, "descriptors: block rows do not cover the sector");
     if (!s.d_desc.alloc(V.n_blocks)) return set_error(ED_ERR_NOMEM, "descriptors: device allocation");
     if (cudaMemcpy(s.d_desc.p, desc.data(), desc.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice) != cudaSuccess)
         return set_error(ED_ERR_CUDA, "descriptors: upload");

@@ -8,8 +8,9 @@ namespace ed {
 // Per-thread sums of products for the Lanczos dot products.  FP64 vectors: FP64 fused
 // multiply-adds.  FP32 vectors: each product is split exactly into a float pair (fma gives the
 // rounding error) and added with Knuth's TwoSum into a float-float sum, so a thread's partial
-// sum carries about 48 bits; the CTA and sector reductions then run in FP64.  This keeps the
-// FP64 units (1/64 of the FP32 rate on this part) off the per-row path.
+// sum carries about 48 bits.  The CTA reduction of a chunk stays in float-float (only its result
+// is converted), and the reduction over chunks runs in FP64.  This keeps the FP64 units (a small
+// fraction of the FP32 rate on this part) off the per-row and per-chunk paths.
 template <typename R>
 struct Accum;
 
@@ -34,6 +35,15 @@ struct Accum<float> {
         hi = t;
     }
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+    // this += o, both float-float (TwoSum of the high parts, low parts added to the error term)
+    __device__ __forceinline__ void add(float ohi, float olo) {
+        const float t = __fadd_rn(hi, ohi);
+        const float bv = __fsub_rn(t, hi);
+        const float te = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bv)), __fsub_rn(ohi, bv));
+        const float e = __fadd_rn(te, __fadd_rn(lo, olo));
+        hi = __fadd_rn(t, e);
+        lo = __fsub_rn(e, __fsub_rn(hi, t));
+    }
 };
 
 template <typename R>
@@ -360,18 +370,20 @@ __device__ __forceinline__ void gather4_block(const typename Vec<R, CPLX>::T* __
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
-template <typename R, bool CPLX>
+// XIN: the caller has already loaded x_i into (xir, xii).
+template <typename R, bool CPLX, int ROWS = 0, bool XIN = false>
 __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
                                             uint64_t key, const BlockDesc* __restrict__ D,
                                             const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
     const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
     const int Ns = S.Ns, N = S.N;
-    ld<R, CPLX>(x, i, xir, xii);
+    if constexpr (!XIN) ld<R, CPLX>(x, i, xir, xii);
     const uint32_t dc = compress_spins(d, h);
     // hot words of the descriptor: {hmask, m_rung, m_legadj, m_legd2}, {mode|nhop|ncand|nwrap, wrap, start}
     const uint4 dw0 = reinterpret_cast<const uint4*>(D)[0];
     const uint4 dw1 = reinterpret_cast<const uint4*>(D)[1];
-    const bool row_free = (dw1.x & 255u) == kModeFree;
+    // ROWS: 0 decides per row from the descriptor; kRowsFree / kRowsCand fix the block kind at compile time
+    const bool row_free = ROWS == 0 ? ((dw1.x & 255u) == kModeFree) : (ROWS == kRowsFree);
     const int nhop = (dw1.x >> 8) & 255u, nwrap = dw1.x >> 24;
     const int wlo[2] = {(int)(dw1.y & 255u), (int)((dw1.y >> 16) & 255u)};
     const int whi[2] = {(int)((dw1.y >> 8) & 255u), (int)(dw1.y >> 24)};
@@ -499,7 +511,8 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
             const R wt = (hw.w & 255u) ? w[1] : w[0];
             if (wt == R(0) || hmode == kModeAbsent) continue;
             const R coef = ((hw.w >> 24) == 1u ? -wt : wt) * sqNi;
-            if (hmode == kModeGeneric) {
+            // (blocks with such hops are orbit-walk blocks: the kind-specialised kernels never see one)
+            if (ROWS == 0 && hmode == kModeGeneric) {
                 const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
                 const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
                 add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
@@ -551,6 +564,16 @@ __device__ __forceinline__ void hv_row_any(const SectorView& S, const HvTables<R
     const BlockDesc* D = row_desc(S, tb.comb, (uint32_t)(key >> 32), staged);
     if (D->mode == kModeGeneric) hv_row<R, CPLX>(S, tb, w, i, x, outr, outi, xir, xii);
     else hv_row_fast<R, CPLX>(S, tb, w, i, key, D, x, outr, outi, xir, xii);
+}
+
+// Stage one block descriptor in shared memory (all threads of the CTA call this).
+__device__ __forceinline__ void stage_block(const BlockDesc* __restrict__ src, BlockDesc* sdesc) {
+    __syncthreads();  // the previous chunk's rows are done with sdesc
+    const int words = (int)(sizeof(BlockDesc) / sizeof(uint4));
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(sdesc);
+    for (int t = threadIdx.x; t < words; t += blockDim.x) d4[t] = s4[t];
+    __syncthreads();
 }
 
 // Stage the block descriptor of row `first` in shared memory (all threads of the CTA call this).

@@ -63,7 +63,40 @@ inline int grid_for(int64_t work, int threads, int sms, int per_sm = 8) {
 }
 
 constexpr int kHvThreads = 256;
-constexpr int kReduceSlots = 4;  // FP64 partial sums per CTA in the fused Lanczos step
+constexpr int kReduceSlots = 4;  // FP64 partial sums per chunk in the fused Lanczos step
+// Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
+// (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
+constexpr int kChunkRows = 4096;
+
+// Row kinds of the fused step: each kind has its own kernel (and register budget).
+enum RowKind : int {
+    kRowsFree = 1,     // blocks with a trivial stabiliser: colex deltas, no orbit lookups
+    kRowsCand = 2,     // blocks with a small stabiliser: coset candidates and bitmap lookups
+    kRowsGeneric = 3,  // everything else (and sectors without descriptors): the orbit walk
+};
+
+// Rows [start, start + count) of one block (block = descriptor index, -1 without descriptors).
+struct BlockSpan {
+    int64_t start, count;
+    int32_t block;
+    int32_t kind;
+};
+
+struct BatchChunk {
+    int32_t sec;
+    int32_t block;       // descriptor of the chunk's block (every row of a chunk is in one block), or -1
+    int64_t begin, end;  // rows of sector `sec`
+};
+
+// Chunk tables of a step layout (one sector, or a batch of sectors): all chunks sector-major in
+// row order (the partial sums are indexed by chunk), and the chunk ids grouped by row kind.
+struct ChunkPlan {
+    std::vector<BatchChunk> chunks;
+    std::vector<int> kind_idx;
+    int kind_first[4] = {0, 0, 0, 0};
+    int kind_count[4] = {0, 0, 0, 0};
+    std::vector<int> cfirst, ccount;  // per sector
+};
 
 struct Sector {
     SectorView view{};
@@ -74,8 +107,10 @@ struct Sector {
     bool built = false;
     int device = 0;
     int num_sms = 152;
-    int hv_grid = 0;             // persistent grid of the H.v kernels
-    int hv_minb = 3;             // launch variant of the fused step kernel (minimum resident CTAs per SM)
+    int hv_grid = 0;             // persistent grid of the H.v kernels (free-row step kernel)
+    int hv_minb = 3;             // launch variant of the free-row step kernel (minimum resident CTAs per SM)
+    int other_grid = 0;          // grid of the other row kinds' step kernels
+    std::vector<BlockSpan> spans;  // host copy of the blocks' row ranges and kinds
     DevBuf<uint32_t> d_comb;     // [33][33]
     DevBuf<uint32_t> d_rank_tab; // [4][Nd+1][256]
     DevBuf<BlockInfo> d_blocks;
@@ -91,15 +126,12 @@ struct Sector {
     int n_chunks = 0;
     DevBuf<SectorView> d_self;
     DevBuf<int64_t> d_offs;
-    DevBuf<struct BatchChunk> d_chunks;
+    DevBuf<BatchChunk> d_chunks;
+    DevBuf<int> d_kidx;
+    int kind_first[4] = {0, 0, 0, 0};
+    int kind_count[4] = {0, 0, 0, 0};
     DevBuf<int> d_cfirst, d_ccount;
     DevBuf<BlockDesc> d_desc;    // fast-row descriptors
-};
-
-struct BatchChunk {
-    int32_t sec;
-    int32_t pad;
-    int64_t begin, end;  // rows of sector `sec`
 };
 
 // ed_basis.cu
@@ -126,6 +158,32 @@ int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* 
 int single_setup(Sector& s);
 int build_descriptors(Sector& s);
 int set_launch(Sector& s, int minb, int ctas_per_sm);
+void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& plan);
+
+// ed_step_free.cu / ed_step_rest.cu: the fused step kernel of one row kind over a list of chunks
+struct StepArgs {
+    const SectorView* views;
+    const int64_t* offs;
+    const BatchChunk* chunks;
+    const int* idx;  // chunk ids of this kind
+    int count;
+    int grid;
+    size_t smem;
+    HvWeights w;
+    void* v;
+    void* vprev;
+    void* other;
+    int first;
+    const double* scal;
+    int stride;
+    int k;
+    double* partials;
+};
+int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st);
+int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st);
+int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st);
+int step_free_occupancy(int minb, size_t smem);
+int step_rest_occupancy(size_t smem);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,

@@ -1,0 +1,15 @@
+// ed_step_rest.cu -- fused step kernels for rows of blocks with a non-trivial stabiliser
+// (coset candidates + bitmap lookups) and for rows that take the orbit walk.
+#include "ed_step.cuh"
+
+namespace ed {
+
+int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st) { return step_kind_dtype<3, kRowsCand>(dtype, a, st); }
+
+int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st) {
+    return step_kind_dtype<3, kRowsGeneric>(dtype, a, st);
+}
+
+int step_rest_occupancy(size_t smem) { return step_kind_occupancy<3, kRowsCand>(smem); }
+
+}  // namespace ed

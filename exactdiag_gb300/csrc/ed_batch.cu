@@ -19,6 +19,14 @@
 
 namespace ed {
 
+// Step flag (scal[2k+3] until a_{k+1} overwrites it): how the update pass finishes v_{k+1}.
+constexpr double kFlagOk = 0.0;            // v_{k+1} = (y - a v) / b
+constexpr double kFlagBreakdown = 1.0;     // b < kBreakdown: v_{k+1} = y - a v, the recursion has ended
+constexpr double kFlagExactPending = 2.0;  // v_{k+1} = y - a v and its exact norm, then b, then the scaling
+constexpr double kFlagScale = 3.0;         // exact b known: v_{k+1} /= b
+constexpr double kBreakdown = 1e-8;        // cython_lanczos_diagonalization.pyx:68-77 stops below this b
+constexpr double kCancel = 1e-6;
+
 // One CTA of kScalarThreads per sector: a_k, b_{k+1} from the sector's chunk partials.  Each thread
 // sums a fixed strided subset of chunks in four independent partial sums (loads stay in flight);
 // the order depends only on the chunk count, so every launch configuration gives the same bits.
@@ -30,6 +38,9 @@ __global__ void __launch_bounds__(kScalarThreads)
                            int norm_mode, int norm_off) {
     __shared__ double red[kReduceSlots][32];
     const int s = blockIdx.x;
+    double* X = scal + (int64_t)s * stride;
+    // norm_mode 2 runs only for sectors whose step left the exact norm pending (uniform per CTA)
+    if (norm_mode == 2 && X[2 * k + 3] != kFlagExactPending) return;
     const int cnt = ccount[s];
     const double2* P = reinterpret_cast<const double2*>(partials + (int64_t)cfirst[s] * kReduceSlots);
     double t[4][kReduceSlots] = {};
@@ -75,17 +86,31 @@ __global__ void __launch_bounds__(kScalarThreads)
             tot[q] = 0.0;
             for (int i = 0; i < nw; ++i) tot[q] += red[q][i];
         }
-        double* X = scal + (int64_t)s * stride;
-        if (norm_mode) {
+        if (norm_mode == 1) {
             X[norm_off] = sqrt(tot[3]);  // |v0|
             return;
         }
+        if (norm_mode == 2) {  // b = |y - a v| summed by the update pass
+            const double b = sqrt(tot[3]);
+            X[2 * k + 2] = b;
+            X[2 * k + 3] = (b < kBreakdown) ? kFlagBreakdown : kFlagScale;
+            return;
+        }
+        // b^2 = |y - a v|^2 = |y|^2 - 2a<v,y> + a^2|v|^2 from the one-pass sums; when the terms cancel
+        // to fewer than about 10 significant digits (y close to a v: a start vector near an
+        // eigenvector) the exact norm is taken by a second pass instead
         const double a = tot[0];
         const double nn = tot[1] - 2.0 * a * tot[2] + a * a * tot[3];
-        const double b = sqrt(nn > 0.0 ? nn : 0.0);
+        const double size = tot[1] + a * a * tot[3];
         X[2 * k + 1] = a;
+        if (nn <= kCancel * size) {
+            X[2 * k + 2] = sqrt(nn > 0.0 ? nn : 0.0);
+            X[2 * k + 3] = kFlagExactPending;
+            return;
+        }
+        const double b = sqrt(nn);
         X[2 * k + 2] = b;
-        X[2 * k + 3] = (b < 1e-8) ? 1.0 : 0.0;
+        X[2 * k + 3] = (b < kBreakdown) ? kFlagBreakdown : kFlagOk;
     }
 }
 
@@ -115,7 +140,7 @@ template <typename R, bool CPLX>
 __global__ void __launch_bounds__(kUpdThreads)
     lanczos_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks, int nchunks,
                           void* v, void* other, const double* __restrict__ scal, int stride, int k, int mode,
-                          int norm_off) {
+                          int norm_off, double* __restrict__ partials) {
     using T = typename Vec<R, CPLX>::T;
     constexpr int kComp = 16 / sizeof(R);                   // real components per 16-byte vector
     constexpr int kRowsPerVec = 16 / sizeof(T);             // rows per 16-byte vector
@@ -124,9 +149,12 @@ __global__ void __launch_bounds__(kUpdThreads)
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
         const double* X = scal + (int64_t)ch.sec * stride;
-        T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(v, offs[ch.sec])) + ch.begin;
-        T* y = mode == 1 ? x : reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
+        // mode 1 scales v by 1/|v0|; mode 3 scales v_{k+1} by the exact 1/b where the step asked for it
+        if (mode == 3 && X[2 * k + 3] != kFlagScale) continue;
+        T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(mode == 3 ? other : v, offs[ch.sec])) + ch.begin;
+        T* y = (mode == 1 || mode == 3) ? x : reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
         R a, inv;
+        bool exact = false;
         // FP32 vectors take the reciprocal in FP32 (the FP64 units are slow on this part)
         auto recip = [](double b) -> R {
             if constexpr (sizeof(R) == 4) return __frcp_rn((float)b);
@@ -136,10 +164,16 @@ __global__ void __launch_bounds__(kUpdThreads)
             const double nv = X[norm_off];
             a = R(0);
             inv = nv > 0.0 ? recip(nv) : R(0);
+        } else if (mode == 3) {
+            a = R(0);
+            inv = recip(X[2 * k + 2]);
         } else {
+            const double flag = X[2 * k + 3];
             a = (R)X[2 * k + 1];
-            inv = X[2 * k + 3] != 0.0 ? R(1) : recip(X[2 * k + 2]);
+            inv = flag != kFlagOk ? R(1) : recip(X[2 * k + 2]);
+            exact = flag == kFlagExactPending;
         }
+        double nrm = 0.0;  // |v_{k+1}|^2 of this thread's rows when the exact norm is pending
         const int rows = (int)(ch.end - ch.begin);
         // rows before the first 16-byte boundary (chunks start where blocks start) go row by row
         const uintptr_t ax = reinterpret_cast<uintptr_t>(x), ay = reinterpret_cast<uintptr_t>(y);
@@ -152,7 +186,9 @@ __global__ void __launch_bounds__(kUpdThreads)
             R vr, vi, yr, yi;
             ld<R, CPLX>(x, i, vr, vi);
             ld<R, CPLX>(y, i, yr, yi);
-            st<R, CPLX>(y, i, (yr - a * vr) * inv, (yi - a * vi) * inv);
+            const R nr = (yr - a * vr) * inv, ni = (yi - a * vi) * inv;
+            st<R, CPLX>(y, i, nr, ni);
+            if (exact) nrm += (double)nr * (double)nr + (CPLX ? (double)ni * (double)ni : 0.0);
         }
         int done = head;
         if (head < rows) {
@@ -178,7 +214,10 @@ __global__ void __launch_bounds__(kUpdThreads)
                         const R* xv = reinterpret_cast<const R*>(&xa[u]);
                         R* yv = reinterpret_cast<R*>(&ya[u]);
 #pragma unroll
-                        for (int e = 0; e < kComp; ++e) yv[e] = (yv[e] - a * xv[e]) * inv;
+                        for (int e = 0; e < kComp; ++e) {
+                            yv[e] = (yv[e] - a * xv[e]) * inv;
+                            if (exact) nrm += (double)yv[e] * (double)yv[e];
+                        }
                         __stcs(ys + q, ya[u]);
                     }
                 }
@@ -189,7 +228,13 @@ __global__ void __launch_bounds__(kUpdThreads)
             R vr, vi, yr, yi;
             ld<R, CPLX>(x, i, vr, vi);
             ld<R, CPLX>(y, i, yr, yi);
-            st<R, CPLX>(y, i, (yr - a * vr) * inv, (yi - a * vi) * inv);
+            const R nr = (yr - a * vr) * inv, ni = (yi - a * vi) * inv;
+            st<R, CPLX>(y, i, nr, ni);
+            if (exact) nrm += (double)nr * (double)nr + (CPLX ? (double)ni * (double)ni : 0.0);
+        }
+        if (exact) {  // uniform over the CTA: the flag belongs to the chunk's sector
+            double tot[kReduceSlots] = {0.0, 0.0, 0.0, nrm};
+            chunk_reduce(tot, partials + (int64_t)c * kReduceSlots);
         }
     }
 }
@@ -296,7 +341,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1,
                                                            stride - 1);
     lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef,
-                                                                 stride, 0, 1, stride - 1);
+                                                                 stride, 0, 1, stride - 1, nullptr);
     ED_CHECK_LAUNCH("batch start vectors");
     cudaStream_t cap = st;
     cudaStream_t priv = nullptr;
@@ -327,7 +372,12 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         }
         lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
         lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
-                                                                      stride, k, 0, 0);
+                                                                      stride, k, 0, 0, partials.p);
+        // sectors whose b needs the exact norm: b from the update pass's sums, then v_{k+1} /= b
+        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 2,
+                                                                 0);
+        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
+                                                                      stride, k, 3, 0, nullptr);
     }
     if (use_graph) {
         cudaGraph_t graph = nullptr;
@@ -447,8 +497,13 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
 
 template <typename R, bool CPLX>
 static void single_update_typed(const Sector& s, const void* v, void* vnext, const double* scal, cudaStream_t st) {
-    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks,
-                                                                 const_cast<void*>(v), vnext, scal, 0, 0, 0, 0);
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(
+        s.d_offs.p, s.d_chunks.p, s.n_chunks, const_cast<void*>(v), vnext, scal, 0, 0, 0, 0, s.d_partials.p);
+    // when the step left the exact norm pending: b from the update pass's sums, then v_{k+1} /= b
+    lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p,
+                                                         const_cast<double*>(scal), 0, 0, 2, 0);
+    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(
+        s.d_offs.p, s.d_chunks.p, s.n_chunks, const_cast<void*>(v), vnext, scal, 0, 0, 3, 0, nullptr);
 }
 
 int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st) {
@@ -477,7 +532,7 @@ static void single_norm_typed(const Sector& s, void* x, double* norm, cudaStream
                                                                 s.d_partials.p);
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, norm, 0, 0, 1, 0);
     lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x, nullptr,
-                                                                 norm, 0, 0, 1, 0);
+                                                                 norm, 0, 0, 1, 0, nullptr);
 }
 
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* /*partials*/, cudaStream_t st) {

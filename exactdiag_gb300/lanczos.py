@@ -90,7 +90,7 @@ def ritz_vector(run: LanczosRun, v0: torch.Tensor, coeffs: np.ndarray) -> torch.
 
 
 def ground_state(sector: DeviceSector, weights, num_steps: int, precision: str = "mixed", seed: int = 0,
-                 refine_steps: int = 12, v0: torch.Tensor | None = None, use_graph: bool = True) -> dict:
+                 refine_steps: int = 32, v0: torch.Tensor | None = None, use_graph: bool = True) -> dict:
     """Ground energy of a sector.
 
     precision "fp64": plain FP64 Lanczos; E0 = lowest Ritz value.

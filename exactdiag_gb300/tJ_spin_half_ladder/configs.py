@@ -310,4 +310,7 @@ def _get_spectrum_figure_suffix(hamiltonian_config: Hamiltonian_Config, spectrum
     ws_string = f"_ws{spectrum_config.omega_min:g},{spectrum_config.omega_max:g},{spectrum_config.omega_steps:g}"
     broad_string = f"_broad{spectrum_config.broadening}"
     vecs_string = f"_vecs{spectrum_config.num_lanczos_vecs}"
-    return f"{operator_name_suffix}{q_string}{ws_string}{broad_string}{vecs_string}_{weight_string}"
+    # FP64 results keep the reference's file names; mixed-precision ones are stored beside them
+    precision_string = "_mixed" if getattr(hamiltonian_config, "precision", "fp64") == "mixed" else ""
+    return (f"{operator_name_suffix}{q_string}{ws_string}{broad_string}{vecs_string}_{weight_string}"
+            f"{precision_string}")

@@ -62,3 +62,13 @@ def seeded_vector(n, seed, complex_):
 
 def fixture_sector(d):
     return (d["num_rungs"], d["num_holes"], d["num_down_spins"], d["symmetry_qs"][0], d["symmetry_qs"][1])
+
+
+@pytest.fixture()
+def in_tmp(tmp_path, monkeypatch):
+    """Run in a temporary folder (the API writes its cache files under ./calculations)."""
+    monkeypatch.chdir(tmp_path)
+    from exactdiag_gb300.tJ_spin_half_ladder import matrix_setup
+
+    yield tmp_path
+    matrix_setup.clear_sector_cache()

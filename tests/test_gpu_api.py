@@ -16,15 +16,6 @@ def torch(cuda):
     return cuda
 
 
-@pytest.fixture()
-def in_tmp(tmp_path, monkeypatch):
-    monkeypatch.chdir(tmp_path)
-    from exactdiag_gb300.tJ_spin_half_ladder import matrix_setup
-
-    yield tmp_path
-    matrix_setup.clear_sector_cache()
-
-
 def _sector(key):
     from exactdiag_gb300.engine import DeviceSector
 

@@ -1,0 +1,101 @@
+"""GPU: the measured configurations at full size, where the plain FP64 GPU path is the oracle.
+
+* 2x12, two holes, all 24 momentum sectors (about 8.1e6 representatives each): the mixed-precision
+  ground energy (FP32 Lanczos, FP64 reductions, FP64 Ritz vector + refinement) against the plain
+  FP64 Lanczos ground energy, relative difference <= 1e-10.
+* 2x12 S^z_q spectra at k=(0,0): all 24 (q_x, q_y), m=150, omega = linspace(0, 6, 2000), eta=0.05;
+  the batched recursion against 24 sequential ones, absolute difference <= 1e-6.
+  (The mixed ground energy is refined by FP64 Lanczos steps from its Ritz vector.)
+* undoped 2x14 (about 1.43e6 representatives) -> spectral_function_minus into the one-hole sectors
+  (about 2.0e7 each), all 28 (q_x, q_y), m=200, omega = linspace(-4, 8, 4000): complex64 vectors
+  with FP64 reductions against complex128, and batched against sequential on a subset of q.
+
+Seeded synthetic start vectors (np.random.default_rng(seed).uniform(-1, 1, n)) throughout.
+"""
+
+import shutil
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
+
+
+def _spectrum_config(L, Nh, name, omega_min, omega_max, steps, m, precision="fp64"):
+    from exactdiag_gb300.tJ_spin_half_ladder import configs
+
+    return configs.Full_Spectrum_Config(
+        hamiltonian={"num_rungs": L, "num_holes": Nh, "weights": W, "symmetry_qs": {"leg": 0, "rung": 0},
+                     "num_threads": 1, "precision": precision},
+        eigenpair={"num_eigenpairs": 3},
+        spectrum={"name": name, "operator_symmetry_qs": {"leg": 0, "rung": 0}, "broadening": 0.05,
+                  "omega_min": omega_min, "omega_max": omega_max, "omega_steps": steps, "num_lanczos_vecs": m})
+
+
+def test_2x12_all_sectors_mixed_ground_energy_matches_fp64(cuda):
+    from exactdiag_gb300.engine import DeviceSector
+    from exactdiag_gb300.lanczos import ground_state
+
+    worst = 0.0
+    for kx in range(12):
+        for ky in (0, 1):
+            sec = DeviceSector(12, 2, 11, kx, ky)
+            g64 = ground_state(sec, W, 200, precision="fp64", seed=0)
+            gmx = ground_state(sec, W, 200, precision="mixed", seed=0)
+            rel = abs(gmx["E0"] - g64["E0"]) / abs(g64["E0"])
+            print(f"2x12 k=({kx},{ky}) E0 fp64 {g64['E0']:.15f} mixed {gmx['E0']:.15f} rel {rel:.2e} "
+                  f"residual {gmx['residual']:.2e}")
+            worst = max(worst, rel)
+            assert rel <= 1e-10, ((kx, ky), g64["E0"], gmx["E0"], rel)
+            del sec
+    print(f"2x12 worst relative ground-energy difference mixed vs FP64: {worst:.3e}")
+
+
+def test_2x12_szq_spectra_batched_equals_sequential(cuda, in_tmp):
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+
+    cfg = _spectrum_config(12, 2, "Szq", 0.0, 6.0, 2000, 150)
+    ws_b, sp_b, _ = api.get_Szq_spectra(cfg, limited_qs=False, batched=True)
+    shutil.rmtree(in_tmp / "calculations")
+    ws_s, sp_s, _ = api.get_Szq_spectra(cfg, limited_qs=False, batched=False)
+    assert sp_b.shape == (12, 2, 2000)
+    assert np.all(np.isfinite(sp_b)) and np.max(sp_b) > 0
+    diff = float(np.max(np.abs(sp_b - sp_s)))
+    print(f"2x12 Szq batched vs sequential max |diff| = {diff:.3e} (max spectrum {np.max(sp_b):.3e})")
+    assert diff <= 1e-6
+
+
+def test_undoped_2x14_spectral_function_minus_mixed_vs_fp64(cuda, in_tmp):
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+
+    mixed = _spectrum_config(14, 0, "spectral_function_minus", -4.0, 8.0, 4000, 200, precision="mixed")
+    ws_m, sp_m, _ = api.get_spectral_function_spectra(mixed, limited_qs=False, batched=True)
+    full = _spectrum_config(14, 0, "spectral_function_minus", -4.0, 8.0, 4000, 200, precision="fp64")
+    ws_f, sp_f, _ = api.get_spectral_function_spectra(full, limited_qs=False, batched=True)
+    assert sp_m.shape == sp_f.shape and sp_m.shape[-1] == 4000
+    assert np.all(np.isfinite(sp_m)) and np.max(sp_f) > 0
+    d = np.abs(sp_m - sp_f).reshape(-1, sp_f.shape[-1])
+    f = np.abs(sp_f).reshape(-1, sp_f.shape[-1])
+    rel = float(np.max(d) / np.max(f))
+    l1 = float(np.sum(d) / np.sum(f))
+    print(f"undoped 2x14 c_minus spectra, complex64 vs complex128: max |diff| / max = {rel:.3e}, "
+          f"sum |diff| / sum = {l1:.3e}")
+    for q in range(d.shape[0]):
+        print(f"  q {q}: max {np.max(d[q]) / max(np.max(f), 1e-300):.2e}  L1 {np.sum(d[q]) / max(np.sum(f[q]), 1e-300):.2e}"
+              f"  weight {np.sum(f[q]):.3e}")
+    # complex64 vectors through 200 unreorthogonalised recursion steps: a few percent of the peak,
+    # the size of the FP64 recursion's own truncation error at this length (m=150 against m=200)
+    assert rel <= 5e-2 and l1 <= 5e-2
+
+
+def test_undoped_2x14_spectral_function_minus_batched_equals_sequential(cuda, in_tmp):
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+
+    cfg = _spectrum_config(14, 0, "spectral_function_minus", -4.0, 8.0, 4000, 200, precision="mixed")
+    ws_b, sp_b, _ = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=True)
+    shutil.rmtree(in_tmp / "calculations")
+    ws_s, sp_s, _ = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=False)
+    diff = float(np.max(np.abs(sp_b - sp_s)))
+    assert diff <= 1e-6

@@ -1,0 +1,51 @@
+"""GPU: the fused Lanczos step kernels (one per block kind) against the plain H.v kernel.
+
+ed_lanczos_hv with no previous vector writes y = H v and the step's partial sums; y must equal
+ed_hv's H v (which the core tests pin to the oracle and to the reference-faithful orbit walk), and
+<v, Hv> must equal the FP64 dot product of the two vectors.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import seeded_vector
+
+pytestmark = pytest.mark.gpu
+
+W = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
+SMALL = [(6, 2, 5, kx, ky) for kx in range(6) for ky in (0, 1)] + [(7, 3, 5, 2, 1), (8, 4, 6, 3, 0), (6, 0, 6, 1, 1),
+                                                                   (8, 1, 7, 5, 1), (5, 5, 0, 0, 0)]
+FULL = [(12, 2, 11, kx, ky) for kx in range(12) for ky in (0, 1)]
+
+
+def _check(torch, key, precision, tol):
+    from exactdiag_gb300.engine import DeviceSector
+
+    sec = DeviceSector(*key)
+    dt = sec.dtype(precision)
+    x = seeded_vector(sec.n, 17, not sec.is_real)
+    v = torch.as_tensor(x if not sec.is_real else x.real, device=sec.device).to(dt)
+    ref = sec.hv(v, W)
+    y = torch.zeros_like(v)
+    scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
+    sec.lanczos_hv(W, v, None, y, scal[0:4])
+    torch.cuda.synchronize()
+    scale = max(1.0, float(torch.max(torch.abs(ref)).item()))
+    err = float(torch.max(torch.abs(y - ref)).item())
+    assert err <= tol * scale, (key, precision, err)
+    a = float(scal[1].item())
+    a_ref = float(torch.vdot(v.to(torch.complex128 if v.is_complex() else torch.float64),
+                             ref.to(torch.complex128 if v.is_complex() else torch.float64)).real.item())
+    assert abs(a - a_ref) <= 1e-9 * max(1.0, abs(a_ref)) * (1 if precision == "fp64" else 1e3), (key, a, a_ref)
+
+
+@pytest.mark.parametrize("key", SMALL)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_step_kernel_equals_hv_small(cuda, key, precision):
+    _check(cuda, key, precision, 1e-12 if precision == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_step_kernel_equals_hv_2x12_all_sectors(cuda, precision):
+    for key in FULL:
+        _check(cuda, key, precision, 1e-12 if precision == "fp64" else 1e-6)

@@ -40,7 +40,7 @@ METRIC = "Lanczos steps/s & HÂ·v HBM GB/s, 2Ã—14 t-J: mixed vs FP64 GPU at Î”Eâ‰
 UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
-KERNEL_VERSION = "v5"  # the H.v kernel generation the committed traffic figure was captured on
+KERNEL_VERSION = "v6"  # the H.v kernel generation the committed traffic figure was captured on
 
 
 def workload_name(sector) -> str:
@@ -166,7 +166,13 @@ def run_engine(args, rank: int, world: int) -> dict | None:
 
     def timed_steps(precision: str):
         dt = sec.dtype(precision)
-        tuned[precision] = autotune.tune(sec, WEIGHTS, dt, use_cache=False)
+        if args.launch:
+            minb, ctas = (int(t) for t in args.launch.split(","))
+            autotune.set_launch(sec, minb, ctas)
+            tuned[precision] = {"min_ctas_per_sm": minb, "ctas_per_sm": ctas, "grid": autotune.get_launch(sec)[1],
+                                "fixed": True}
+        else:
+            tuned[precision] = autotune.tune(sec, WEIGHTS, dt, use_cache=False)
         rng = np.random.default_rng(0)
         v0 = torch.as_tensor(rng.uniform(-1, 1, n), device=dev).to(dt)
         buf = [v0.clone(), torch.zeros_like(v0)]
@@ -272,10 +278,10 @@ def run_engine(args, rank: int, world: int) -> dict | None:
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic,
-                     "kernel": "lanczos_hv_kernel<float,false> + lanczos_scalars_kernel (ed_lanczos_hv)",
+                     "kernel": "lanczos_hv_kernel<float,false,*,kind> for each block kind + lanczos_scalars_kernel (ed_lanczos_hv)",
                      "algorithmic_bytes_per_launch": n * bytes_per_row},
         "e2e": e2e,
-        "gpu_launches": 3 * K,
+        "gpu_launches": K * autotune.step_launches(sec),
         "clocks": clocks,
         "cpu_baseline": None if args.no_cpu else cpu_baseline(args),
     }
@@ -442,6 +448,9 @@ def main() -> None:
     ap.add_argument("--cpu-sample-rows", type=int, default=4000)
     ap.add_argument("--cpu-vec-sample", type=int, default=4_000_000)
     ap.add_argument("--sector", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--launch", default=None, metavar="MINB,CTAS",
+                    help="fix the free-row step kernel's launch (register variant 3|4, CTAs per SM, 0 = all that fit) "
+                         "instead of tuning it")
     args = ap.parse_args()
     if args.sector:
         global SECTOR

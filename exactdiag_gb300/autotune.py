@@ -69,6 +69,19 @@ def get_launch(sector: DeviceSector) -> tuple[int, int]:
     return a.value, g.value
 
 
+def row_kinds(sector: DeviceSector) -> tuple[int, int, int]:
+    """Chunks of the fused step per row kind (free, stabiliser-resolved, orbit walk)."""
+    c = (ctypes.c_int * 3)()
+    nat.check("ed_sector_row_kinds", sector._lib.ed_sector_row_kinds(sector.handle, c))
+    return int(c[0]), int(c[1]), int(c[2])
+
+
+def step_launches(sector: DeviceSector) -> int:
+    """Kernel launches of one ed_lanczos_step: one fused H.v kernel per row kind present, the
+    scalar reduction, and the update (flat pass, exact-norm pass, exact b, scaling pass)."""
+    return sum(1 for c in row_kinds(sector) if c > 0) + 1 + 4
+
+
 def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_cache: bool = True) -> dict:
     """Apply the fastest launch configuration for this sector shape; returns the record used."""
     key = _key(sector, dtype)

@@ -166,6 +166,15 @@ int ed_sector_get_launch(const ed_sector* h, int* min_ctas_per_sm, int* grid) {
     return ED_OK;
 }
 
+int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
+    if (!h || !counts) return set_error(ED_ERR_INVALID, "ed_sector_row_kinds: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_row_kinds: basis not built");
+    counts[0] = h->s.kind_count[kRowsFree];
+    counts[1] = h->s.kind_count[kRowsCand];
+    counts[2] = h->s.kind_count[kRowsGeneric];
+    return ED_OK;
+}
+
 int ed_basis_size(const ed_sector* h, int64_t* n) {
     if (!h || !n) return set_error(ED_ERR_INVALID, "ed_basis_size: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_basis_size: basis not built");

@@ -130,111 +130,203 @@ __global__ void norm_partials_kernel(const int64_t* __restrict__ offs, const Bat
     }
 }
 
-// mode 0: v_next = (y - a v) / b (step update); mode 1: v *= 1/|v0| (start vector).
-// Every real component (the real and imaginary parts alike) is updated the same way, so a chunk
-// whose rows start on a 16-byte boundary is moved as 16-byte vectors, all of a thread's loads
-// issued before its stores; the ragged tail of the last chunk goes row by row.
+// The update v_{k+1} = (y - a v) / b.  Every real component (real and imaginary parts alike) is
+// updated the same way, so rows from the first 16-byte boundary on move as 16-byte vectors, a
+// thread's loads all issued before its stores; rows before the boundary and the tail go one by one.
 constexpr int kUpdThreads = 256;
 
+template <typename R>
+__device__ __forceinline__ R recip_r(double b) {
+    if constexpr (sizeof(R) == 4) return __frcp_rn((float)b);  // FP32 vectors: no FP64 division
+    else return 1.0 / b;
+}
+
+// y[i] = (y[i] - a x[i]) * inv for i in [0, rows), by one CTA; EXACT also sums |y[i]|^2 (FP64).
+// Called once per chunk: kept out of line so each caller's register budget stays its own.
+template <typename R, bool CPLX, bool EXACT>
+__device__ __noinline__ void update_rows(const typename Vec<R, CPLX>::T* x, typename Vec<R, CPLX>::T* y,
+                                            int rows, R a, R inv, double& nrm) {
+    using T = typename Vec<R, CPLX>::T;
+    constexpr int kComp = 16 / sizeof(R);                        // real components per 16-byte vector
+    constexpr int kRowsPerVec = 16 / sizeof(T);                  // rows per 16-byte vector
+    auto row = [&](int i) {
+        R vr, vi, yr, yi;
+        ld<R, CPLX>(x, i, vr, vi);
+        ld<R, CPLX>(y, i, yr, yi);
+        const R nr = (yr - a * vr) * inv, ni = (yi - a * vi) * inv;
+        st<R, CPLX>(y, i, nr, ni);
+        if constexpr (EXACT) nrm += (double)nr * (double)nr + (CPLX ? (double)ni * (double)ni : 0.0);
+    };
+    const uintptr_t ax = reinterpret_cast<uintptr_t>(x), ay = reinterpret_cast<uintptr_t>(y);
+    int head = rows;
+    if (((ax ^ ay) & 15u) == 0 && (ax % sizeof(T)) == 0) {
+        head = (int)(((16u - (ax & 15u)) & 15u) / sizeof(T));
+        if (head > rows) head = rows;
+    }
+    for (int i = threadIdx.x; i < head; i += kUpdThreads) row(i);
+    int done = head;
+    if (head < rows) {
+        const int nvec = (rows - head) / kRowsPerVec;
+        const uint4* xs = reinterpret_cast<const uint4*>(x + head);
+        uint4* ys = reinterpret_cast<uint4*>(y + head);
+        for (int q0 = threadIdx.x; q0 < nvec; q0 += 4 * kUpdThreads) {
+            uint4 xa[4], ya[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = q0 + u * kUpdThreads;
+                if (q < nvec) {
+                    xa[u] = __ldcs(xs + q);
+                    ya[u] = __ldcs(ys + q);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = q0 + u * kUpdThreads;
+                if (q < nvec) {
+                    const R* xv = reinterpret_cast<const R*>(&xa[u]);
+                    R* yv = reinterpret_cast<R*>(&ya[u]);
+#pragma unroll
+                    for (int e = 0; e < kComp; ++e) {
+                        yv[e] = (yv[e] - a * xv[e]) * inv;
+                        if constexpr (EXACT) nrm += (double)yv[e] * (double)yv[e];
+                    }
+                    __stcs(ys + q, ya[u]);
+                }
+            }
+        }
+        done = head + nvec * kRowsPerVec;
+    }
+    for (int i = done + threadIdx.x; i < rows; i += kUpdThreads) row(i);
+}
+
+// Chunked update over every chunk (batched recursions and start vectors): mode 0 the step update
+// (sectors whose exact norm is pending are left to lanczos_exact_kernel), mode 1 v *= 1/|v0|.
 template <typename R, bool CPLX>
-__global__ void __launch_bounds__(kUpdThreads)
+__global__ void __launch_bounds__(kUpdThreads, 4)
     lanczos_update_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks, int nchunks,
                           void* v, void* other, const double* __restrict__ scal, int stride, int k, int mode,
-                          int norm_off, double* __restrict__ partials) {
+                          int norm_off) {
     using T = typename Vec<R, CPLX>::T;
-    constexpr int kComp = 16 / sizeof(R);                   // real components per 16-byte vector
-    constexpr int kRowsPerVec = 16 / sizeof(T);             // rows per 16-byte vector
-    constexpr int kIt = kChunkRows / kRowsPerVec / kUpdThreads;  // vectors per thread in a full chunk
-    static_assert(kChunkRows % (kRowsPerVec * kUpdThreads) == 0, "chunk must split into whole vectors");
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const BatchChunk ch = chunks[c];
         const double* X = scal + (int64_t)ch.sec * stride;
-        // mode 1 scales v by 1/|v0|; mode 3 scales v_{k+1} by the exact 1/b where the step asked for it
-        if (mode == 3 && X[2 * k + 3] != kFlagScale) continue;
-        T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(mode == 3 ? other : v, offs[ch.sec])) + ch.begin;
-        T* y = (mode == 1 || mode == 3) ? x : reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
-        R a, inv;
-        bool exact = false;
-        // FP32 vectors take the reciprocal in FP32 (the FP64 units are slow on this part)
-        auto recip = [](double b) -> R {
-            if constexpr (sizeof(R) == 4) return __frcp_rn((float)b);
-            else return 1.0 / b;
-        };
+        T* x = reinterpret_cast<T*>(vec_at<R, CPLX>(v, offs[ch.sec])) + ch.begin;
+        double nrm = 0.0;
         if (mode == 1) {
             const double nv = X[norm_off];
-            a = R(0);
-            inv = nv > 0.0 ? recip(nv) : R(0);
-        } else if (mode == 3) {
-            a = R(0);
-            inv = recip(X[2 * k + 2]);
-        } else {
-            const double flag = X[2 * k + 3];
-            a = (R)X[2 * k + 1];
-            inv = flag != kFlagOk ? R(1) : recip(X[2 * k + 2]);
-            exact = flag == kFlagExactPending;
+            update_rows<R, CPLX, false>(x, x, (int)(ch.end - ch.begin), R(0), nv > 0.0 ? recip_r<R>(nv) : R(0),
+                                        nrm);
+            continue;
         }
-        double nrm = 0.0;  // |v_{k+1}|^2 of this thread's rows when the exact norm is pending
-        const int rows = (int)(ch.end - ch.begin);
-        // rows before the first 16-byte boundary (chunks start where blocks start) go row by row
-        const uintptr_t ax = reinterpret_cast<uintptr_t>(x), ay = reinterpret_cast<uintptr_t>(y);
-        int head = rows;
-        if (((ax ^ ay) & 15u) == 0 && (ax % sizeof(T)) == 0) {
-            head = (int)(((16u - (ax & 15u)) & 15u) / sizeof(T));
-            if (head > rows) head = rows;
-        }
-        for (int i = threadIdx.x; i < head; i += kUpdThreads) {
-            R vr, vi, yr, yi;
-            ld<R, CPLX>(x, i, vr, vi);
-            ld<R, CPLX>(y, i, yr, yi);
-            const R nr = (yr - a * vr) * inv, ni = (yi - a * vi) * inv;
-            st<R, CPLX>(y, i, nr, ni);
-            if (exact) nrm += (double)nr * (double)nr + (CPLX ? (double)ni * (double)ni : 0.0);
-        }
-        int done = head;
-        if (head < rows) {
-            const int nvec = (rows - head) / kRowsPerVec;
-            const uint4* xs = reinterpret_cast<const uint4*>(x + head);
-            uint4* ys = reinterpret_cast<uint4*>(y + head);
-            constexpr int kBatch = kIt < 4 ? kIt : 4;  // 16-byte vectors per array in flight per thread
-#pragma unroll 1
-            for (int u0 = 0; u0 < kIt; u0 += kBatch) {
-                uint4 xa[kBatch], ya[kBatch];
+        const double flag = X[2 * k + 3];
+        if (flag == kFlagExactPending) continue;
+        T* y = reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[ch.sec])) + ch.begin;
+        update_rows<R, CPLX, false>(x, y, (int)(ch.end - ch.begin), (R)X[2 * k + 1],
+                                    flag != kFlagOk ? R(1) : recip_r<R>(X[2 * k + 2]), nrm);
+    }
+}
+
+// Single-sector step update as one flat stream over the vector (no chunk table): every thread
+// handles whole 16-byte vectors, four per array in flight.  Left to lanczos_exact_kernel when the
+// step's exact norm is pending.
+template <typename R, bool CPLX>
+__global__ void __launch_bounds__(kUpdThreads, 4)
+    lanczos_update_flat_kernel(int64_t n, const void* __restrict__ v, void* __restrict__ other,
+                               const double* __restrict__ X) {
+    using T = typename Vec<R, CPLX>::T;
+    constexpr int kComp = 16 / sizeof(R);
+    constexpr int kRowsPerVec = 16 / sizeof(T);
+    const double flag = X[3];
+    if (flag == kFlagExactPending) return;
+    const R a = (R)X[1];
+    const R inv = flag != kFlagOk ? R(1) : recip_r<R>(X[2]);
+    const T* x = reinterpret_cast<const T*>(v);
+    T* y = reinterpret_cast<T*>(other);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    const uintptr_t ax = reinterpret_cast<uintptr_t>(x), ay = reinterpret_cast<uintptr_t>(y);
+    int64_t head = n;
+    if (((ax ^ ay) & 15u) == 0 && (ax % sizeof(T)) == 0) {
+        head = (int64_t)(((16u - (ax & 15u)) & 15u) / sizeof(T));
+        if (head > n) head = n;
+    }
+    auto row = [&](int64_t i) {
+        R vr, vi, yr, yi;
+        ld<R, CPLX>(x, i, vr, vi);
+        ld<R, CPLX>(y, i, yr, yi);
+        st<R, CPLX>(y, i, (yr - a * vr) * inv, (yi - a * vi) * inv);
+    };
+    for (int64_t i = tid; i < head; i += nth) row(i);
+    if (head >= n) return;
+    const int64_t nvec = (n - head) / kRowsPerVec;
+    const uint4* xs = reinterpret_cast<const uint4*>(x + head);
+    uint4* ys = reinterpret_cast<uint4*>(y + head);
+    for (int64_t q0 = tid; q0 < nvec; q0 += 4 * nth) {
+        uint4 xa[4], ya[4];
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) {
-                    const int q = threadIdx.x + (u0 + u) * kUpdThreads;
-                    if (q < nvec) {
-                        xa[u] = __ldcs(xs + q);
-                        ya[u] = mode == 1 ? xa[u] : __ldcs(ys + q);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kBatch; ++u) {
-                    const int q = threadIdx.x + (u0 + u) * kUpdThreads;
-                    if (q < nvec) {
-                        const R* xv = reinterpret_cast<const R*>(&xa[u]);
-                        R* yv = reinterpret_cast<R*>(&ya[u]);
-#pragma unroll
-                        for (int e = 0; e < kComp; ++e) {
-                            yv[e] = (yv[e] - a * xv[e]) * inv;
-                            if (exact) nrm += (double)yv[e] * (double)yv[e];
-                        }
-                        __stcs(ys + q, ya[u]);
-                    }
-                }
+        for (int u = 0; u < 4; ++u) {
+            const int64_t q = q0 + u * nth;
+            if (q < nvec) {
+                xa[u] = __ldcs(xs + q);
+                ya[u] = __ldcs(ys + q);
             }
-            done = head + nvec * kRowsPerVec;
         }
-        for (int i = done + threadIdx.x; i < rows; i += kUpdThreads) {
-            R vr, vi, yr, yi;
-            ld<R, CPLX>(x, i, vr, vi);
-            ld<R, CPLX>(y, i, yr, yi);
-            const R nr = (yr - a * vr) * inv, ni = (yi - a * vi) * inv;
-            st<R, CPLX>(y, i, nr, ni);
-            if (exact) nrm += (double)nr * (double)nr + (CPLX ? (double)ni * (double)ni : 0.0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t q = q0 + u * nth;
+            if (q < nvec) {
+                const R* xv = reinterpret_cast<const R*>(&xa[u]);
+                R* yv = reinterpret_cast<R*>(&ya[u]);
+#pragma unroll
+                for (int e = 0; e < kComp; ++e) yv[e] = (yv[e] - a * xv[e]) * inv;
+                __stcs(ys + q, ya[u]);
+            }
         }
-        if (exact) {  // uniform over the CTA: the flag belongs to the chunk's sector
+    }
+    for (int64_t i = head + nvec * kRowsPerVec + tid; i < n; i += nth) row(i);
+}
+
+// Sectors whose step left the exact norm pending (rare: a start vector near an eigenvector):
+// v_{k+1} = y - a v and its per-chunk |v_{k+1}|^2 partial sums.  The flag is read per sector,
+// so CTAs skip the other sectors' chunk ranges at once.
+template <typename R, bool CPLX>
+__global__ void __launch_bounds__(kUpdThreads, 4)
+    lanczos_exact_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+                         const int* __restrict__ cfirst, const int* __restrict__ ccount, int nsec, void* v,
+                         void* other, const double* __restrict__ scal, int stride, int k,
+                         double* __restrict__ partials) {
+    using T = typename Vec<R, CPLX>::T;
+    for (int s = 0; s < nsec; ++s) {
+        const double* X = scal + (int64_t)s * stride;
+        if (X[2 * k + 3] != kFlagExactPending) continue;
+        const R a = (R)X[2 * k + 1];
+        for (int c = cfirst[s] + blockIdx.x; c < cfirst[s] + ccount[s]; c += gridDim.x) {
+            const BatchChunk ch = chunks[c];
+            const T* x = reinterpret_cast<const T*>(vec_at<R, CPLX>(v, offs[s])) + ch.begin;
+            T* y = reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[s])) + ch.begin;
+            double nrm = 0.0;
+            update_rows<R, CPLX, true>(x, y, (int)(ch.end - ch.begin), a, R(1), nrm);
             double tot[kReduceSlots] = {0.0, 0.0, 0.0, nrm};
             chunk_reduce(tot, partials + (int64_t)c * kReduceSlots);
+        }
+    }
+}
+
+// After the exact b is known: v_{k+1} /= b for the sectors flagged kFlagScale.
+template <typename R, bool CPLX>
+__global__ void __launch_bounds__(kUpdThreads, 4)
+    lanczos_scale_kernel(const int64_t* __restrict__ offs, const BatchChunk* __restrict__ chunks,
+                         const int* __restrict__ cfirst, const int* __restrict__ ccount, int nsec, void* other,
+                         const double* __restrict__ scal, int stride, int k) {
+    using T = typename Vec<R, CPLX>::T;
+    for (int s = 0; s < nsec; ++s) {
+        const double* X = scal + (int64_t)s * stride;
+        if (X[2 * k + 3] != kFlagScale) continue;
+        const R inv = recip_r<R>(X[2 * k + 2]);
+        for (int c = cfirst[s] + blockIdx.x; c < cfirst[s] + ccount[s]; c += gridDim.x) {
+            const BatchChunk ch = chunks[c];
+            T* y = reinterpret_cast<T*>(vec_at<R, CPLX>(other, offs[s])) + ch.begin;
+            double nrm = 0.0;
+            update_rows<R, CPLX, false>(y, y, (int)(ch.end - ch.begin), R(0), inv, nrm);
         }
     }
 }
@@ -341,7 +433,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1,
                                                            stride - 1);
     lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef,
-                                                                 stride, 0, 1, stride - 1, nullptr);
+                                                                 stride, 0, 1, stride - 1);
     ED_CHECK_LAUNCH("batch start vectors");
     cudaStream_t cap = st;
     cudaStream_t priv = nullptr;
@@ -372,12 +464,14 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         }
         lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
         lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
-                                                                      stride, k, 0, 0, partials.p);
-        // sectors whose b needs the exact norm: b from the update pass's sums, then v_{k+1} /= b
+                                                                      stride, k, 0, 0);
+        // sectors whose b needs the exact norm: y - a v and its norm, b, then v_{k+1} /= b
+        lanczos_exact_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, dcfirst.p, dccount.p, nsec,
+                                                                     v, other, coef, stride, k, partials.p);
         lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 2,
                                                                  0);
-        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
-                                                                      stride, k, 3, 0, nullptr);
+        lanczos_scale_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, dcfirst.p, dccount.p, nsec,
+                                                                     other, coef, stride, k);
     }
     if (use_graph) {
         cudaGraph_t graph = nullptr;
@@ -497,13 +591,16 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
 
 template <typename R, bool CPLX>
 static void single_update_typed(const Sector& s, const void* v, void* vnext, const double* scal, cudaStream_t st) {
-    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(
-        s.d_offs.p, s.d_chunks.p, s.n_chunks, const_cast<void*>(v), vnext, scal, 0, 0, 0, 0, s.d_partials.p);
-    // when the step left the exact norm pending: b from the update pass's sums, then v_{k+1} /= b
+    const int flat_grid = s.num_sms * 8;
+    lanczos_update_flat_kernel<R, CPLX><<<flat_grid, kUpdThreads, 0, st>>>(s.view.n, v, vnext, scal);
+    // when the step left the exact norm pending: y - a v and its norm, b, then v_{k+1} /= b
+    lanczos_exact_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(
+        s.d_offs.p, s.d_chunks.p, s.d_cfirst.p, s.d_ccount.p, 1, const_cast<void*>(v), vnext, scal, 0, 0,
+        s.d_partials.p);
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p,
                                                          const_cast<double*>(scal), 0, 0, 2, 0);
-    lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(
-        s.d_offs.p, s.d_chunks.p, s.n_chunks, const_cast<void*>(v), vnext, scal, 0, 0, 3, 0, nullptr);
+    lanczos_scale_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.d_cfirst.p,
+                                                                        s.d_ccount.p, 1, vnext, scal, 0, 0);
 }
 
 int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st) {
@@ -532,7 +629,7 @@ static void single_norm_typed(const Sector& s, void* x, double* norm, cudaStream
                                                                 s.d_partials.p);
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, norm, 0, 0, 1, 0);
     lanczos_update_kernel<R, CPLX><<<step_grid(s), kUpdThreads, 0, st>>>(s.d_offs.p, s.d_chunks.p, s.n_chunks, x, nullptr,
-                                                                 norm, 0, 0, 1, 0, nullptr);
+                                                                 norm, 0, 0, 1, 0);
 }
 
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* /*partials*/, cudaStream_t st) {

@@ -11,6 +11,8 @@ from __future__ import annotations
 
 import copy
 import logging
+import os
+import pathlib
 from functools import partial
 
 import numpy as np
@@ -90,12 +92,52 @@ def setup_excitation_operator(initial_config):
     return get_operator, final_h, final_h.setup()
 
 
+BASIS_MAP_FILE = "Sz_local-momentum_map.dat"  # matrix_setup.pyx:390
+
+
+def save_basis_map(path, sparse: np.ndarray, orbit: np.ndarray) -> None:
+    """Write a basis in the reference's binary format (basis_indexing.h:128-146): the number of
+    representatives as an unsigned 64-bit count, then dense_to_sparse as int64 and
+    num_sparse_states_in_dense as int32, native little-endian."""
+    path = pathlib.Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    n = len(sparse)
+    if len(orbit) != n:
+        raise ValueError("dense_to_sparse and num_sparse_states_in_dense differ in length")
+    tmp = path.with_name(path.name + ".tmp")
+    with open(tmp, "wb") as f:
+        np.array([n], dtype="<u8").tofile(f)
+        np.ascontiguousarray(sparse, dtype="<i8").tofile(f)
+        np.ascontiguousarray(orbit, dtype="<i4").tofile(f)
+    os.replace(tmp, path)
+
+
+def load_basis_map(path) -> tuple[np.ndarray, np.ndarray]:
+    """Read a basis written by the reference or by save_basis_map (basis_indexing.h:72-100)."""
+    path = pathlib.Path(path)
+    with open(path, "rb") as f:
+        head = np.fromfile(f, dtype="<u8", count=1)
+        if len(head) != 1:
+            raise ValueError(f"{path}: truncated basis file")
+        n = int(head[0])
+        sparse = np.fromfile(f, dtype="<i8", count=n)
+        orbit = np.fromfile(f, dtype="<i4", count=n)
+        rest = f.read(1)
+    if len(sparse) != n or len(orbit) != n or rest:
+        raise ValueError(f"{path}: basis file does not hold {n} representatives")
+    return sparse, orbit
+
+
 class Py_Basis_Index_Map:
     """Host view of a device basis with the reference's query methods (basis_indexing.pxd:40-53)."""
 
     def __init__(self, sparse: np.ndarray, orbit: np.ndarray):
         self.dense_to_sparse = sparse
         self.num_sparse_in_dense = orbit
+
+    def save(self, path) -> None:
+        """The basis .dat file (basis_indexing.h:128-146)."""
+        save_basis_map(path, self.dense_to_sparse, self.num_sparse_in_dense)
 
     def get_num_states(self) -> int:
         return len(self.dense_to_sparse)
@@ -180,7 +222,19 @@ class Py_Symmetry_Generator:
 
 
 def py_get_ladder_translators(config: configs.Hamiltonian_Config):
-    """(translator, basis map, symmetry generator) (matrix_setup.pyx:377-406); the basis is built on the GPU."""
+    """(translator, basis map, symmetry generator) (matrix_setup.pyx:377-406).
+
+    The basis is built on the GPU.  Like the reference (basis_indexing.h:58-66), the basis file in the
+    sector's calculation folder is written when absent; when present (written by the reference or by
+    this package) it must hold the same basis, else ValueError names the file.
+    """
     sec = sector_of(config)
     sparse, orbit = sec.export_basis()
+    path = config.get_calc_folder() / BASIS_MAP_FILE
+    if path.exists():
+        f_sparse, f_orbit = load_basis_map(path)
+        if not (np.array_equal(f_sparse, sparse) and np.array_equal(f_orbit, orbit.astype(np.int32))):
+            raise ValueError(f"{path} holds a different basis than sector {config.sector_key()}")
+    else:
+        save_basis_map(path, sparse, orbit)
     return Py_State_Index_Amplitude_Translator(config), Py_Basis_Index_Map(sparse, orbit), Py_Symmetry_Generator(config)

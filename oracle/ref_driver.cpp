@@ -250,4 +250,32 @@ int ref_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz
     }
 }
 
+// general/basis_indexing.h:128-146 Basis_Index_Map::save (the basis .dat file).
+int ref_basis_save(const char* path, const int64_t* d2s, const int32_t* orb, int64_t n) {
+    try {
+        make_map(d2s, orb, n)->save(std::filesystem::path(path));
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// general/basis_indexing.h:72-100 Basis_Index_Map(path): read a basis .dat file.
+int ref_basis_load(const char* path, int64_t* out_sparse, int32_t* out_orbit, int64_t cap, int64_t* n_out) {
+    try {
+        Basis_Index_Map m{std::filesystem::path(path)};
+        const int64_t n = m.get_num_states();
+        *n_out = n;
+        if (!out_sparse) return 0;
+        if (n > cap) return -2;
+        for (int64_t i = 0; i < n; ++i) {
+            out_sparse[i] = m.get_sparse(i);
+            out_orbit[i] = m.get_num_sparse_in_dense(i);
+        }
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
 }  // extern "C"

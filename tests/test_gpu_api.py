@@ -133,6 +133,24 @@ def test_drop_in_hamiltonian_dot_and_translators(torch, oracle, in_tmp):
     assert bmap.get_dense(-1) == -1 and sym.get_basis_length() == 12
 
 
+def test_translators_write_and_check_the_basis_file(torch, oracle, in_tmp):
+    """get_translators writes the sector's basis .dat like the reference and checks an existing one."""
+    from exactdiag_gb300.tJ_spin_half_ladder import configs
+    from exactdiag_gb300.tJ_spin_half_ladder.matrix_setup import BASIS_MAP_FILE, load_basis_map, save_basis_map
+
+    cfg = configs.Hamiltonian_Config(num_rungs=7, num_holes=2, weights=W, symmetry_qs={"leg": 2, "rung": 0},
+                                     num_threads=1)
+    _, bmap, _ = cfg.get_translators()
+    path = cfg.get_calc_folder() / BASIS_MAP_FILE
+    sp, orb = load_basis_map(path)
+    osp, oorb = oracle.basis(oracle.Sector(7, 2, cfg.num_down_spins, 2, 0))
+    assert np.array_equal(sp, osp) and np.array_equal(orb, oorb.astype(np.int32))
+    cfg.get_translators()  # an existing, matching file is accepted
+    save_basis_map(path, sp[:-1], orb[:-1])
+    with pytest.raises(ValueError, match="different basis"):
+        cfg.get_translators()
+
+
 def test_lanczos_dynamical_response_vs_oracle(torch, oracle, in_tmp):
     """phi = O|gs>, the recursion's coefficients and the continued fraction against the oracle.
 

@@ -123,3 +123,43 @@ def test_continued_fraction_restatement(oracle):
     vec = oracle.continued_fraction(a, b, zs, 2.5)
     for k, z in enumerate(zs):
         assert abs(vec[k] - (-1 / np.pi * 2.5 * oracle.spectral_value_at_z(a, b, z))) < 1e-12
+
+
+def test_basis_map_file_format_matches_reference(oracle, tmp_path):
+    """The basis .dat writer/reader against the reference's own Basis_Index_Map save/load."""
+    import ctypes
+
+    from exactdiag_gb300.tJ_spin_half_ladder.matrix_setup import load_basis_map, save_basis_map
+
+    ref = oracle.ref_lib()
+    if ref is None:
+        pytest.skip("the reference's code is not built here")
+    i64p, i32p = ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)
+    for key in [(6, 2, 5, 1, 1), (8, 2, 7, 0, 0), (5, 0, 5, 2, 0)]:
+        sp, orb = oracle.basis(oracle.Sector(*key))
+        orb = orb.astype(np.int32)
+        ours = tmp_path / f"ours_{key}.dat"
+        save_basis_map(ours, sp, orb)
+        n = ctypes.c_int64()
+        assert ref.ref_basis_load(str(ours).encode(), None, None, ctypes.c_int64(0), ctypes.byref(n)) == 0
+        rs, ro = np.zeros(n.value, np.int64), np.zeros(n.value, np.int32)
+        assert ref.ref_basis_load(str(ours).encode(), rs.ctypes.data_as(i64p), ro.ctypes.data_as(i32p),
+                                  ctypes.c_int64(n.value), ctypes.byref(n)) == 0
+        assert np.array_equal(rs, sp) and np.array_equal(ro, orb)
+        theirs = tmp_path / f"theirs_{key}.dat"
+        assert ref.ref_basis_save(str(theirs).encode(), sp.ctypes.data_as(i64p), orb.ctypes.data_as(i32p),
+                                  ctypes.c_int64(len(sp))) == 0
+        assert theirs.read_bytes() == ours.read_bytes()
+        ls, lo = load_basis_map(theirs)
+        assert np.array_equal(ls, sp) and np.array_equal(lo, orb)
+
+
+def test_basis_map_file_rejects_truncation(tmp_path):
+    from exactdiag_gb300.tJ_spin_half_ladder.matrix_setup import load_basis_map, save_basis_map
+
+    p = tmp_path / "b.dat"
+    save_basis_map(p, np.arange(10, dtype=np.int64), np.full(10, 4, np.int32))
+    data = p.read_bytes()
+    p.write_bytes(data[:-3])
+    with pytest.raises(ValueError):
+        load_basis_map(p)

@@ -4,10 +4,13 @@
 // tJ_spin_half_ladder/matrix_setup.pyx:195-374 (built by
 // general/column_functions.h:150-207 and applied through
 // general/sparse_matrices.py:83-105):
-//   op 0  Szq:                     O = sum_r w_r S^z_r          (matrix_setup.pyx:235-246)
-//   op 1  spectral_function_minus: O = sum_r w_r c_{r,sigma}    (matrix_setup.pyx:302-325)
-// with w_r = base * exp(-i q.r), base = 1/(2 sqrt(N)) resp. 1/sqrt(N), and q.r
-// evaluated per axis in single precision like get_q_dot_r
+//   op 0  Szq:                     O = sum_r w_r S^z_r                  (matrix_setup.pyx:235-246)
+//   op 1  spectral_function_minus: O = sum_r w_r c_{r,sigma}            (matrix_setup.pyx:302-325)
+//   op 2  spectral_function_plus:  O = sum_r w_r c^+_{r,sigma}          (matrix_setup.pyx:281-300)
+//   op 3  current_rung:            O = sum_r w_r c^+_{r'} c_r, r' the rung partner   (:248-263)
+//   op 4  current_leg:             O = sum_r w_r (c^+_{r+x} c_r - c^+_{r-x} c_r)    (:265-279)
+// with w_r = base * exp(-i q.r), base = 1/(2 sqrt(N)), 1/sqrt(N), 1/sqrt(N), i, i, q_y raised by
+// one for current_rung (:251), and q.r evaluated per axis in single precision like get_q_dot_r
 // (general/group/symmetry_generator.h:87-102).
 //
 // Row j of O is the conjugate of column j of the adjoint O^+, which the
@@ -15,16 +18,19 @@
 //   O[j, i] = sum_{r} w_r * sqrt(N_j) * conj(u^{e}/sqrt(N_i)) * s_r
 // where the sum runs over the sites r at which O^+ acts on t_j (every occupied
 // site for Szq, with s_r = +1 up / -1 down; every hole site for c_minus, with
-// s_r = (-1)^{electrons of t_j above r} and the added spin sigma), and
-// (i, N_i, e) is the representative of the resulting configuration in the
-// source sector.  One thread per target row, no atomics.
+// s_r = (-1)^{electrons of t_j above r} and the removed spin sigma re-added;
+// every electron of spin sigma for c_plus, removed; for the currents every
+// bond whose one end is a hole of t_j and whose other end holds the electron
+// that hopped, moved back, with s_r = (-1)^{electrons strictly between} on the
+// leg), and (i, N_i, e) is the representative of the resulting configuration in
+// the source sector.  One thread per target row, no atomics.
 #include "ed_device.cuh"
 
 namespace ed {
 
 struct ExciteParams {
     int op;
-    int add_down;      // c_minus: the removed (pull: re-added) spin is down
+    int add_down;      // c_minus: the removed (pull: re-added) spin is down; c_plus: the added one is
     int qx, qy;
     double wr[kMaxN];  // w_r
     double wi[kMaxN];
@@ -64,16 +70,11 @@ __global__ void __launch_bounds__(kHvThreads)
                 acci += vr * (double)xi + vi * (double)xr;
             }
         } else {
-            uint32_t holes = h;
-            while (holes) {
-                const int r = __ffs(holes) - 1;
-                holes &= holes - 1u;
-                const uint32_t bit = 1u << r;
-                const uint32_t h2 = h ^ bit, d2 = P.add_down ? (d | bit) : d;
+            // one source configuration (h2, d2) reached by O^+ at site r (the operator's site in the
+            // target frame, the startpoint for the currents), with its sign and endpoint weight
+            auto add_term = [&](uint32_t h2, uint32_t d2, int r, double sgn) {
                 const Resolved rv = resolve(S, tb.rank, tb.comb, h2, d2);
-                if (rv.j < 0) continue;
-                const uint32_t above = (r == 31) ? 0u : (~0u << (r + 1));
-                const double sgn = (__popc(occ & above) & 1) ? -1.0 : 1.0;
+                if (rv.j < 0) return;
                 // The reference evaluates this term from the source representative, at the site
                 // rs = g(r) where g maps the new configuration to its lowest image, with w_rs rounded
                 // in single precision; w_r = w_rs * exp(+i q.(rs - r)) exactly.
@@ -91,6 +92,38 @@ __global__ void __launch_bounds__(kHvThreads)
                 ld<R, true>(x, rv.j, xr, xi);
                 accr += vr * (double)xr - vi * (double)xi;
                 acci += vr * (double)xi + vi * (double)xr;
+            };
+            auto above = [](int r) -> uint32_t { return (r == 31) ? 0u : (~0u << (r + 1)); };
+            if (P.op == 1) {  // c_minus: re-add the removed electron at each hole
+                for (uint32_t holes = h; holes; holes &= holes - 1u) {
+                    const int r = __ffs(holes) - 1;
+                    const uint32_t bit = 1u << r;
+                    add_term(h ^ bit, P.add_down ? (d | bit) : d, r, (__popc(occ & above(r)) & 1) ? -1.0 : 1.0);
+                }
+            } else if (P.op == 2) {  // c_plus: remove the added electron at each site holding that spin
+                for (uint32_t el = occ & (P.add_down ? d : ~d); el; el &= el - 1u) {
+                    const int r = __ffs(el) - 1;
+                    const uint32_t bit = 1u << r;
+                    add_term(h | bit, d & ~bit, r, (__popc(occ & above(r)) & 1) ? -1.0 : 1.0);
+                }
+            } else {  // currents: the electron at `end` came from the hole `start`
+                for (uint32_t holes = h; holes; holes &= holes - 1u) {
+                    const int start = __ffs(holes) - 1;
+                    const int nshift = P.op == 3 ? 1 : 2;
+                    for (int k = 0; k < nshift; ++k) {
+                        const int end = P.op == 3 ? (start ^ 1) : ((start + (k == 0 ? 2 : N - 2)) % N);
+                        if (!((occ >> end) & 1u)) continue;
+                        const uint32_t bs = 1u << start, be = 1u << end;
+                        const uint32_t d2 = ((d >> end) & 1u) ? (d ^ be ^ bs) : d;
+                        double sgn = k == 0 ? 1.0 : -1.0;  // endpoint weights (0, 1), (0, -1)
+                        if (P.op == 4) {
+                            const int lo = start < end ? start : end, hi = start < end ? end : start;
+                            const uint32_t between = ((1u << hi) - 1u) & ~((2u << lo) - 1u);
+                            if (__popc(occ & between) & 1) sgn = -sgn;
+                        }
+                        add_term(h ^ bs ^ be, d2, start, sgn);
+                    }
+                }
             }
         }
         st<R, true>(y, j, (R)accr, (R)acci);
@@ -113,14 +146,15 @@ int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, 
     const SectorView& T = dst.view;
     if (S.L != T.L) return set_error(ED_ERR_INVALID, "ed_excitation_apply: sectors of different ladders");
     const int L = S.L;
+    const int qye = op == 3 ? qy + 1 : qy;
     const int kx2 = (((src.kx_raw + qx + (L - 1) / 2) % L) + L) % L - (L - 1) / 2;
-    const int ky2 = (((S.ky + qy) % 2) + 2) % 2;
+    const int ky2 = (((S.ky + qye) % 2) + 2) % 2;
     if (((kx2 % L) + L) % L != T.kx || ky2 != T.ky)
         return set_error(ED_ERR_INVALID, "ed_excitation_apply: target sector momentum does not match k + q");
     ExciteParams P{};
     P.op = op;
     P.qx = qx;
-    P.qy = qy;
+    P.qy = op == 3 ? qy + 1 : qy;  // current_rung (matrix_setup.pyx:251)
     double base;
     if (op == 0) {
         if (T.Nh != S.Nh || T.Nd != S.Nd) return set_error(ED_ERR_INVALID, "ed_excitation_apply: Szq keeps Nh, Nd");
@@ -131,13 +165,28 @@ int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, 
             return set_error(ED_ERR_INVALID, "ed_excitation_apply: spectral_function_minus target must have one more "
                                              "hole and the removed spin");
         base = 1.0 / std::sqrt((double)S.N);
+    } else if (op == 2) {
+        P.add_down = initial_sz2 > 0;
+        if (S.Nh < 1 || T.Nh != S.Nh - 1 || T.Nd != S.Nd + (P.add_down ? 1 : 0))
+            return set_error(ED_ERR_INVALID, "ed_excitation_apply: spectral_function_plus target must have one hole "
+                                             "less and the added spin");
+        base = 1.0 / std::sqrt((double)S.N);
+    } else if (op == 3 || op == 4) {
+        if (T.Nh != S.Nh || T.Nd != S.Nd)
+            return set_error(ED_ERR_INVALID, "ed_excitation_apply: currents keep Nh, Nd");
+        base = 1.0;
     } else {
         return set_error(ED_ERR_INVALID, "ed_excitation_apply: unknown operator");
     }
     for (int r = 0; r < S.N; ++r) {
-        const double qr = q_dot_r(r, qx, qy, L);
-        P.wr[r] = base * std::cos(qr);
-        P.wi[r] = -base * std::sin(qr);
+        const double qr = q_dot_r(r, qx, P.qy, L);
+        if (op == 3 || op == 4) {  // i exp(-i q.r)
+            P.wr[r] = std::sin(qr);
+            P.wi[r] = std::cos(qr);
+        } else {
+            P.wr[r] = base * std::cos(qr);
+            P.wi[r] = -base * std::sin(qr);
+        }
     }
     if (T.n == 0) return ED_OK;
     if (dtype != ED_C128 && dtype != ED_C64)

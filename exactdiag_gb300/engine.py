@@ -48,6 +48,11 @@ def weights_tuple(weights) -> tuple[float, float, float, float]:
     return w
 
 
+# ed_excitation_apply operator codes (tJ_spin_half_ladder/matrix_setup.pyx:235-325)
+EXCITATION_OPS = {"Szq": 0, "spectral_function_minus": 1, "spectral_function_plus": 2, "current_rung": 3,
+                  "current_leg": 4}
+
+
 @dataclass(frozen=True)
 class SectorKey:
     num_rungs: int
@@ -182,7 +187,7 @@ class DeviceSector:
     def excite_into(self, dst: "DeviceSector", name: str, qx: int, qy: int, initial_sz2: int, x: torch.Tensor,
                     out: torch.Tensor | None = None) -> torch.Tensor:
         """y = O x into sector dst (ed_excitation_apply); x, y complex."""
-        op = {"Szq": 0, "spectral_function_minus": 1}[str(name)]
+        op = EXCITATION_OPS[str(name)]
         if x.dtype not in (torch.complex128, torch.complex64) or x.numel() != self.n or not x.is_cuda:
             raise ValueError("x must be a complex CUDA tensor of the source sector's length")
         code = _CODE_OF_TORCH[x.dtype]

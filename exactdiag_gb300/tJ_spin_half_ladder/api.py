@@ -64,8 +64,8 @@ def get_excitation_spectrum(config: configs.Full_Spectrum_Config, limited_qs: bo
     base_name = config.spectrum.name
     info = {}
     if base_name in {"current_rung", "current_leg"}:
-        raise NotImplementedError(f"{base_name} is not implemented on the GPU engine")
-    if base_name == "Szq":
+        ws, spectrum = ld.get_spectrum(config)
+    elif base_name == "Szq":
         ws, spectrum, info = get_Szq_spectra(config=config, limited_qs=limited_qs, batched=batched)
     elif base_name in {"spectral_function_plus", "spectral_function_minus"}:
         ws, spectrum, info = get_spectral_function_spectra(config=config, limited_qs=limited_qs, batched=batched)
@@ -172,8 +172,6 @@ def get_spectral_function_spectra(config: configs.Full_Spectrum_Config, limited_
         (configs.Spectrum_Name.SPECTRAL_FUNCTION_PLUS, config.hamiltonian.num_holes > 0),
         (configs.Spectrum_Name.SPECTRAL_FUNCTION_MINUS, config.hamiltonian.num_holes < config.hamiltonian.num_nodes),
     ]
-    if plus_minus_conditions[0][1]:
-        raise NotImplementedError("spectral_function_plus (states with holes) is not implemented on the GPU engine")
     qs_list = list(itertools.product(qxs, qys))
     shape = [sum(c for _, c in plus_minus_conditions), len(qs_list), config.spectrum.omega_steps]
     spectra = np.empty(shape, dtype=float)
@@ -193,7 +191,15 @@ def get_spectral_function_spectra(config: configs.Full_Spectrum_Config, limited_
             c.spectrum.name = name
             cfgs.append(c)
             slots.append((o - int(not plus_minus_conditions[0][1]), i))
-    results = _spectra_batched(cfgs) if batched else [ld.get_spectrum(c) for c in cfgs]
+    if batched:  # one batched recursion per operator: plus and minus targets differ in Nh and Nd
+        results = [None] * len(cfgs)
+        for name, _ in plus_minus_conditions:
+            pick = [k for k, c in enumerate(cfgs) if c.spectrum.name == name]
+            if pick:
+                for k, r in zip(pick, _spectra_batched([cfgs[k] for k in pick])):
+                    results[k] = r
+    else:
+        results = [ld.get_spectrum(c) for c in cfgs]
     for (o, i), (w, s) in zip(slots, results):
         ws[o, i, :], spectra[o, i, :] = w, s
     return ws, spectra, {"qs_list": qs_list}

@@ -24,7 +24,9 @@ from exactdiag_gb300.tJ_spin_half_ladder import configs
 _logger = logging.getLogger(__name__)
 _SECTORS: dict[tuple, DeviceSector] = {}
 
-IMPLEMENTED_OPERATORS = (configs.Spectrum_Name.SZQ, configs.Spectrum_Name.SPECTRAL_FUNCTION_MINUS)
+IMPLEMENTED_OPERATORS = (configs.Spectrum_Name.SZQ, configs.Spectrum_Name.SPECTRAL_FUNCTION_MINUS,
+                         configs.Spectrum_Name.SPECTRAL_FUNCTION_PLUS, configs.Spectrum_Name.CURRENT_RUNG,
+                         configs.Spectrum_Name.CURRENT_LEG)
 
 
 def get_sector(num_rungs: int, num_holes: int, num_down_spins: int, kx: int, ky: int) -> DeviceSector:
@@ -58,21 +60,31 @@ def _make_hamiltonian(config: configs.Hamiltonian_Config) -> Device_Hamiltonian:
 
 
 def target_sector_config(initial_config, name, qx: int, qy: int) -> configs.Hamiltonian_Config:
-    """Final Hamiltonian config of an excitation (matrix_setup.pyx:263-330)."""
+    """Final Hamiltonian config of an excitation (matrix_setup.pyx:248-330)."""
     h = initial_config.hamiltonian
     final = copy.deepcopy(h)
     L = h.num_rungs
     kx, ky = h.symmetry_qs.leg, h.symmetry_qs.rung
-    if name == configs.Spectrum_Name.SZQ:
+    if name in (configs.Spectrum_Name.SZQ, configs.Spectrum_Name.CURRENT_LEG):
         pass
+    elif name == configs.Spectrum_Name.CURRENT_RUNG:
+        qy += 1  # the rung current's hopping-direction sign is carried by the target's rung parity (:251)
     elif name == configs.Spectrum_Name.SPECTRAL_FUNCTION_MINUS:
         final.num_holes += 1
         if h.total_spin_projection <= 0:
             final.total_spin_projection += 1
         else:
             final.total_spin_projection -= 1
+    elif name == configs.Spectrum_Name.SPECTRAL_FUNCTION_PLUS:
+        if h.num_holes < 1:
+            raise ValueError("spectral_function_plus needs a hole to fill")
+        final.num_holes -= 1
+        if h.total_spin_projection > 0:
+            final.total_spin_projection -= 1
+        else:
+            final.total_spin_projection += 1
     else:
-        raise NotImplementedError(f"{name}: only {[str(n) for n in IMPLEMENTED_OPERATORS]} run on the GPU engine")
+        raise ValueError(f"{name} not supported")
     final.symmetry_qs = configs.Quantum_Numbers(leg=(kx + qx + (L - 1) // 2) % L - (L - 1) // 2, rung=(ky + qy) % 2)
     return final
 

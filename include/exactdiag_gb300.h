@@ -137,8 +137,16 @@ int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const
  *   op 1: spectral_function_minus = sum_r (1/sqrt(N)) e^{-iq.r} c_{r,sigma},
  *         sigma = down if initial_sz2 <= 0 else up (matrix_setup.pyx:302-325;
  *         dst has Nh+1 holes and the removed spin)
+ *   op 2: spectral_function_plus = sum_r (1/sqrt(N)) e^{-iq.r} c^+_{r,sigma},
+ *         sigma = down if initial_sz2 > 0 else up (matrix_setup.pyx:281-300;
+ *         dst has Nh-1 holes and the added spin)
+ *   op 3: current_rung = sum_r i e^{-iq'.r} c^+_{r'} c_r, r' the rung partner,
+ *         q' = (qx, qy+1) (matrix_setup.pyx:248-263; dst has the same Nh, Nd)
+ *   op 4: current_leg = sum_r i e^{-iq.r} (c^+_{r+x} c_r - c^+_{r-x} c_r)
+ *         (matrix_setup.pyx:265-279; dst has the same Nh, Nd)
  * (qx, qy) are the operator quantum numbers as the matrix setup receives them;
- * dst must be the sector the reference's target rule gives (matrix_setup.pyx:329-330).
+ * dst must be the sector the reference's target rule gives (matrix_setup.pyx:329-330,
+ * with q_y raised by one for current_rung).
  * Vectors are complex: dtype ED_C128 or ED_C64, x of length n(src), y of n(dst).
  * Replaces setup_excitation_operator's stored matrix and its .dot. */
 int ed_excitation_apply(const ed_sector* src, const ed_sector* dst, int op, int qx, int qy, int initial_sz2, int dtype,

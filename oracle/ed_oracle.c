@@ -514,9 +514,12 @@ typedef enum {
     VAL_NO_HOLES = 2,  /* :25-30 */
     VAL_ALL_DOWN = 3,  /* :39-44 */
     VAL_ALL_UP = 4,    /* :32-37 */
+    VAL_ALL_HOLES = 5, /* :46-51 */
 } validator_t;
 
-typedef enum { NEW_SWAP = 0, NEW_KEEP = 1, NEW_ADD_HOLE = 2 } newstate_t;
+/* tJ_spin_half_ladder/matrix_element_functions.pyx: swap, dont_change, add_hole (:112-118),
+ * add_spin_down (:98-103), add_spin_up (:105-110) */
+typedef enum { NEW_SWAP = 0, NEW_KEEP = 1, NEW_ADD_HOLE = 2, NEW_ADD_DOWN = 3, NEW_ADD_UP = 4 } newstate_t;
 
 typedef struct {
     const combos_t *c;
@@ -541,6 +544,10 @@ static int is_valid(validator_t v, const st_t *st, const int16_t *ind, int len) 
     case VAL_ALL_DOWN:
         for (int i = 0; i < len; ++i)
             if (st[ind[i]] != DOWN) return 0;
+        return 1;
+    case VAL_ALL_HOLES:
+        for (int i = 0; i < len; ++i)
+            if (st[ind[i]] != HOLE) return 0;
         return 1;
     default:
         for (int i = 0; i < len; ++i)
@@ -576,8 +583,9 @@ static int column(const ors_t *ini, int64_t col, int64_t sparse, int orbit_size,
         if (r->gen == NEW_SWAP) {
             ns[ind[0]] = st[ind[1]];
             ns[ind[1]] = st[ind[0]];
-        } else if (r->gen == NEW_ADD_HOLE) {
-            for (int i = 0; i < r->c->len; ++i) ns[ind[i]] = HOLE;
+        } else if (r->gen == NEW_ADD_HOLE || r->gen == NEW_ADD_DOWN || r->gen == NEW_ADD_UP) {
+            const st_t v = r->gen == NEW_ADD_HOLE ? HOLE : (r->gen == NEW_ADD_DOWN ? DOWN : UP);
+            for (int i = 0; i < r->c->len; ++i) ns[ind[i]] = v;
         }
         int64_t fs;
         double complex amp;
@@ -657,7 +665,9 @@ static double q_dot_r(int site, int qx, int qy, int L) {
 }
 
 /* Excitation operators (tJ_spin_half_ladder/matrix_setup.pyx:195-374):
- *   op 0: Szq (:235-246), op 1: spectral_function_minus (:302-325).
+ *   op 0: Szq (:235-246), op 1: spectral_function_minus (:302-325),
+ *   op 2: spectral_function_plus (:281-300), op 3: current_rung (:248-263),
+ *   op 4: current_leg (:265-279).
  * (qx, qy) are operator_symmetry_qs as the matrix setup receives them.
  * The final sector (L, Nh2, Nd2, kx2, ky2) and its basis are given by the
  * caller (the target-sector rule is in the Python wrapper). */
@@ -669,14 +679,38 @@ int or_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz2
     if (sector_init(&s, L, Nh, Nd, kx, ky) != OR_OK) return OR_EINVAL;
     if (sector_init(&f, L, Nh2, Nd2, kx2, ky2) != OR_OK) return OR_EINVAL;
     combos_t c;
-    c.n = s.N;
-    c.len = 1;
-    double base = (op == 0) ? 0.5 / sqrt((double)s.N) : 1.0 / sqrt((double)s.N);
-    for (int i = 0; i < s.N; ++i) {
-        c.idx[i][0] = (int16_t)i;
-        double complex ph = cexp(-I * q_dot_r(i, qx, qy, L)); /* matrix_rules_utils.pyx:90-119 */
-        c.wd[i] = 0.0 * ph;
-        c.wo[i] = base * ph;
+    if (op == 3 || op == 4) {
+        /* matrix_rules_utils.pyx:15-87 with startpoints = all sites, reverse=True: [end, start];
+         * startpoint weights (0, i) exp(-i q.r_start) (:90-119), endpoint weights (0, 1) and, for the
+         * leg's second shift, (0, -1).  current_rung raises q_y by one first (matrix_setup.pyx:251). */
+        const int qye = op == 3 ? qy + 1 : qy;
+        static const int rung[1][2] = {{0, 1}};
+        static const int leg[2][2] = {{1, 0}, {-1, 0}};
+        const int (*sh)[2] = op == 3 ? rung : leg;
+        const int nsh = op == 3 ? 1 : 2;
+        c.n = 0;
+        c.len = 2;
+        for (int first = 0; first < s.N; ++first) {
+            const double complex sw = I * cexp(-I * q_dot_r(first, qx, qye, L));
+            for (int k = 0; k < nsh; ++k) {
+                const int end = index_by_relative_shift(s.N, first, sh[k][0], sh[k][1]);
+                c.idx[c.n][0] = (int16_t)end;
+                c.idx[c.n][1] = (int16_t)first;
+                c.wd[c.n] = 0.0 * sw;
+                c.wo[c.n] = (k == 0 ? 1.0 : -1.0) * sw;
+                c.n++;
+            }
+        }
+    } else {
+        c.n = s.N;
+        c.len = 1;
+        double base = (op == 0) ? 0.5 / sqrt((double)s.N) : 1.0 / sqrt((double)s.N);
+        for (int i = 0; i < s.N; ++i) {
+            c.idx[i][0] = (int16_t)i;
+            double complex ph = cexp(-I * q_dot_r(i, qx, qy, L)); /* matrix_rules_utils.pyx:90-119 */
+            c.wd[i] = 0.0 * ph;
+            c.wo[i] = base * ph;
+        }
     }
     rule_t r;
     r.c = &c;
@@ -693,6 +727,16 @@ int or_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz2
         r.valid = (Sz2 <= 0) ? VAL_ALL_DOWN : VAL_ALL_UP;
         r.gen = NEW_ADD_HOLE;
         r.use_sign = 1;
+        r.spin_weights = 0;
+    } else if (op == 2) {
+        r.valid = VAL_ALL_HOLES;
+        r.gen = (Sz2 > 0) ? NEW_ADD_DOWN : NEW_ADD_UP;
+        r.use_sign = 1;
+        r.spin_weights = 0;
+    } else if (op == 3 || op == 4) {
+        r.valid = VAL_HOLE_HOP;
+        r.gen = NEW_SWAP;
+        r.use_sign = op == 4;
         r.spin_weights = 0;
     } else {
         return OR_EINVAL;

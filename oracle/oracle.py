@@ -35,7 +35,7 @@ REF_PATH = HERE / "_ref" / "libedref.so"
 REF_SRC = pathlib.Path(os.environ.get("EXACTDIAG_REF_SRC", "/root/reference/src/exactdiag"))
 
 TERMS = ("tl", "tr", "jl", "jr")
-OPS = {"Szq": 0, "spectral_function_minus": 1}
+OPS = {"Szq": 0, "spectral_function_minus": 1, "spectral_function_plus": 2, "current_rung": 3, "current_leg": 4}
 
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _i32p = ctypes.POINTER(ctypes.c_int32)
@@ -178,14 +178,20 @@ def term_columns(sec: Sector, term: str, bas, triangle: bool = True, impl: str =
 def target_sector(sec: Sector, name: str, qx: int, qy: int) -> Sector:
     """Final sector of an excitation (tJ_spin_half_ladder/matrix_setup.pyx:263-330); (qx, qy) as the setup sees them."""
     L = sec.L
+    if name == "current_rung":
+        qy += 1  # matrix_setup.pyx:251
     kx2 = (sec.kx + qx + (L - 1) // 2) % L - (L - 1) // 2
     ky2 = (sec.ky + qy) % 2
-    if name == "Szq":
+    if name in ("Szq", "current_rung", "current_leg"):
         return Sector(L, sec.Nh, sec.Nd, kx2, ky2)
     if name == "spectral_function_minus":
         if sec.Sz2 <= 0:
             return Sector(L, sec.Nh + 1, sec.Nd - 1, kx2, ky2)
         return Sector(L, sec.Nh + 1, sec.Nd, kx2, ky2)
+    if name == "spectral_function_plus":  # matrix_setup.pyx:281-300: a down spin when Sz > 0, else an up spin
+        if sec.Sz2 > 0:
+            return Sector(L, sec.Nh - 1, sec.Nd + 1, kx2, ky2)
+        return Sector(L, sec.Nh - 1, sec.Nd, kx2, ky2)
     raise ValueError(name)
 
 

@@ -82,6 +82,11 @@ bool valid_all_up(const state_int* s, const pos_int* ind, int len) {
         if (s[ind[i]] != SPIN_UP_VALUE) return false;
     return true;
 }
+bool valid_all_holes(const state_int* s, const pos_int* ind, int len) {
+    for (int i = 0; i < len; ++i)
+        if (s[ind[i]] != HOLE_VALUE) return false;
+    return true;
+}
 // matrix_element_functions.pyx:66-69 -> general/column_functions.h:317 count_commutations.
 int anticommutation_sign(const state_int* s, pos_int n, const vector<pos_int>& ind) {
     int count = count_commutations(s, n, ind, HOLE_VALUE, false);
@@ -99,6 +104,15 @@ void weights_spin_projection(const state_int* s, const vector<pos_int>& ind, VAL
 void add_hole(const state_int* in, state_int* out, pos_int n, const vector<pos_int>& ind) {
     memcpy(out, in, n * sizeof(state_int));
     for (size_t i = 0; i < ind.size(); ++i) out[ind[i]] = HOLE_VALUE;
+}
+// matrix_element_functions.pyx:98-110
+void add_spin_down(const state_int* in, state_int* out, pos_int n, const vector<pos_int>& ind) {
+    memcpy(out, in, n * sizeof(state_int));
+    for (size_t i = 0; i < ind.size(); ++i) out[ind[i]] = SPIN_DOWN_VALUE;
+}
+void add_spin_up(const state_int* in, state_int* out, pos_int n, const vector<pos_int>& ind) {
+    memcpy(out, in, n * sizeof(state_int));
+    for (size_t i = 0; i < ind.size(); ++i) out[ind[i]] = SPIN_UP_VALUE;
 }
 
 // general/matrix_rules_utils.pyx:15-87 (reverse=True) + :136-148 validators.
@@ -214,7 +228,8 @@ int ref_term_columns(int L, int Nh, int Nd, int kx, int ky, int term, int triang
     }
 }
 
-// tJ_spin_half_ladder/matrix_setup.pyx:235-246 (op 0, Szq) and :302-325 (op 1, spectral_function_minus).
+// tJ_spin_half_ladder/matrix_setup.pyx:235-246 (op 0, Szq), :302-325 (op 1, spectral_function_minus),
+// :281-300 (op 2, spectral_function_plus), :248-263 (op 3, current_rung), :265-279 (op 4, current_leg).
 int ref_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz2, const int64_t* d2s,
                            const int32_t* orb, int64_t n, int Nh2, int Nd2, int kx2, int ky2, const int64_t* fd2s,
                            const int32_t* forb, int64_t fn, int qx, int qy, int64_t* colptr, int64_t* rows,
@@ -226,25 +241,53 @@ int ref_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz
         int N = 2 * L;
         vector<vector<pos_int>> idx;
         vector<vector<VALUE_TYPE>> w;
-        double base = op == 0 ? 0.5 / std::sqrt((double)N) : 1.0 / std::sqrt((double)N);
-        vector<int> q{qx, qy};
-        for (int i = 0; i < N; ++i) {
-            idx.push_back({(pos_int)i});
-            // general/matrix_rules_utils.pyx:90-119 get_iqr_weights
-            std::complex<double> qr = s.sym->get_q_dot_r(i, q);
-            std::complex<double> ph = std::exp(std::complex<double>(0, -1) * qr);
-            w.push_back({0.0 * ph, base * ph});
+        if (op == 3 || op == 4) {
+            // general/matrix_rules_utils.pyx:15-87 with startpoint weights (0, i) exp(-i q.r)
+            // (:90-119) and endpoint weights (0, 1), (0, -1); current_rung raises q_y by one
+            vector<int> q{qx, op == 3 ? qy + 1 : qy};
+            std::vector<std::array<int, 2>> shifts = op == 3 ? std::vector<std::array<int, 2>>{{0, 1}}
+                                                             : std::vector<std::array<int, 2>>{{1, 0}, {-1, 0}};
+            for (int first = 0; first < N; ++first) {
+                std::complex<double> qr = s.sym->get_q_dot_r(first, q);
+                std::complex<double> sw = std::complex<double>(0, 1) * std::exp(std::complex<double>(0, -1) * qr);
+                for (size_t k = 0; k < shifts.size(); ++k) {
+                    int shift[2] = {shifts[k][0], shifts[k][1]};
+                    int end = s.sym->get_index_by_relative_shift(first, shift);
+                    idx.push_back({(pos_int)end, (pos_int)first});
+                    std::complex<double> e = k == 0 ? 1.0 : -1.0;
+                    w.push_back({0.0 * sw, sw * e});
+                }
+            }
+        } else {
+            double base = op == 0 ? 0.5 / std::sqrt((double)N) : 1.0 / std::sqrt((double)N);
+            vector<int> q{qx, qy};
+            for (int i = 0; i < N; ++i) {
+                idx.push_back({(pos_int)i});
+                // general/matrix_rules_utils.pyx:90-119 get_iqr_weights
+                std::complex<double> qr = s.sym->get_q_dot_r(i, q);
+                std::complex<double> ph = std::exp(std::complex<double>(0, -1) * qr);
+                w.push_back({0.0 * ph, base * ph});
+            }
         }
         std::shared_ptr<I_Lambda_Matrix_Elements> el;
         if (op == 0) {
             el.reset(new Lambda_Matrix_Elements(f.trans, fmap, N, dont_change, valid_no_holes, nullptr,
                                                 weights_spin_projection, nullptr, idx, w));
-        } else {
+        } else if (op == 1) {
             el.reset(new Lambda_Matrix_Elements(f.trans, fmap, N, add_hole, Sz2 <= 0 ? valid_all_down : valid_all_up,
                                                 nullptr, nullptr, anticommutation_sign, idx, w));
+        } else if (op == 2) {
+            el.reset(new Lambda_Matrix_Elements(f.trans, fmap, N, Sz2 > 0 ? add_spin_down : add_spin_up,
+                                                valid_all_holes, nullptr, nullptr, anticommutation_sign, idx, w));
+        } else if (op == 3 || op == 4) {
+            el.reset(new Lambda_Matrix_Elements(f.trans, fmap, N, static_cast<get_new_state_type*>(::swap),
+                                                valid_hole_hopping, nullptr, nullptr,
+                                                op == 4 ? anticommutation_sign : nullptr, idx, w));
+        } else {
+            return -1;
         }
         Lambda_Column colf(imap, s.trans, el, true);
-        return run_columns(colf, n, colptr, rows, vre, vim, cap, nnz_out, N + 2);
+        return run_columns(colf, n, colptr, rows, vre, vim, cap, nnz_out, (int)idx.size() + 2);
     } catch (...) {
         return -1;
     }

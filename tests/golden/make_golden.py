@@ -14,7 +14,8 @@ Outputs
                            sizes) and y = H x for a seeded x, both computed by
                            the reference's compiled code, plus 30 spectrum-Lanczos
                            coefficients from the numpy restatement on that matrix;
-  excitations.npz          O x for Szq and spectral_function_minus operators.
+  excitations.npz          O x for the Szq, spectral_function_minus, spectral_function_plus,
+                           current_rung and current_leg operators.
 """
 
 from __future__ import annotations
@@ -55,6 +56,12 @@ EXCITATIONS = [
     ((6, 0, 6, 0, 0), "spectral_function_minus", -1, 0),
     ((6, 0, 6, 0, 0), "spectral_function_minus", -2, 1),
     ((5, 1, 4, 0, 1), "spectral_function_minus", -3, 0),
+    ((6, 2, 5, 0, 0), "spectral_function_plus", 1, 0),
+    ((6, 2, 4, 1, 0), "spectral_function_plus", 2, 1),
+    ((6, 2, 5, 1, 1), "current_rung", 2, 1),
+    ((7, 1, 6, 3, 0), "current_rung", -2, 0),
+    ((6, 2, 5, 2, 1), "current_leg", 0, 1),
+    ((8, 2, 7, 0, 0), "current_leg", 4, 0),
 ]
 
 
@@ -117,7 +124,7 @@ def main() -> None:
         ex[f"e{idx}_y"] = op @ x
         ex[f"e{idx}_seed"] = np.array([3000 + idx])
         ex[f"e{idx}_target"] = np.array(fsec.args())
-    ex["cases"] = np.array([[*k, {"Szq": 0, "spectral_function_minus": 1}[n], qx, qy] for k, n, qx, qy in EXCITATIONS])
+    ex["cases"] = np.array([[*k, O.OPS[n], qx, qy] for k, n, qx, qy in EXCITATIONS])
     np.savez_compressed(OUT / "excitations.npz", **ex)
     print("wrote", sorted(p.name for p in OUT.glob("*.npz")), "and reference_fixtures.json")
 

@@ -84,7 +84,7 @@ def test_oracle_matches_golden(oracle, golden_sectors):
 
 
 def test_oracle_excitations_match_golden(oracle, golden_excitations):
-    names = {0: "Szq", 1: "spectral_function_minus"}
+    names = {code: name for name, code in oracle.OPS.items()}
     for idx, case in enumerate(golden_excitations["cases"]):
         L, Nh, Nd, kx, ky, op, qx, qy = (int(v) for v in case)
         sec = oracle.Sector(L, Nh, Nd, kx, ky)
@@ -163,3 +163,33 @@ def test_basis_map_file_rejects_truncation(tmp_path):
     p.write_bytes(data[:-3])
     with pytest.raises(ValueError):
         load_basis_map(p)
+
+
+EXCITATION_SOURCES = [(4, 1, 2, 1, 0), (5, 2, 4, 2, 1), (5, 1, 4, 0, 0), (6, 2, 5, 3, 0), (6, 1, 5, 1, 1),
+                      (6, 0, 6, 2, 0), (4, 2, 2, 0, 1), (7, 3, 5, 1, 0)]
+
+
+@pytest.mark.parametrize("name", ["Szq", "spectral_function_minus", "spectral_function_plus", "current_rung",
+                                  "current_leg"])
+def test_oracle_excitations_bit_exact_against_reference_code(oracle, name):
+    """Operator columns of the restatement against the reference's own column functions."""
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference's code is not built here")
+    cases = 0
+    for key in EXCITATION_SOURCES:
+        sec = oracle.Sector(*key)
+        if name == "spectral_function_plus" and sec.Nh == 0:
+            continue
+        if name == "spectral_function_minus" and sec.Nh == sec.N:
+            continue
+        bas = oracle.basis(sec)
+        for qx in range(sec.L):
+            for qy in (0, 1):
+                fsec = oracle.target_sector(sec, name, qx, qy)
+                fbas = oracle.basis(fsec)
+                a = oracle.excitation_columns(sec, bas, name, qx, qy, fsec, fbas)
+                b = oracle.excitation_columns(sec, bas, name, qx, qy, fsec, fbas, impl="ref")
+                assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (key, qx, qy)
+                assert np.max(np.abs(a[2] - b[2]), initial=0) < 1e-14, (key, qx, qy)
+                cases += 1
+    assert cases > 0

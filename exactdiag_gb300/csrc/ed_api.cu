@@ -166,6 +166,19 @@ int ed_sector_get_launch(const ed_sector* h, int* min_ctas_per_sm, int* grid) {
     return ED_OK;
 }
 
+int ed_position_correlations(const ed_sector* h, int dtype, const void* psi_dev, int kind, int nfixed,
+                             const int* fixed_shifts, double* out_host, void* stream) {
+    if (!h || !psi_dev || !out_host) return set_error(ED_ERR_INVALID, "ed_position_correlations: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_position_correlations: basis not built");
+    if ((dtype == ED_F64 || dtype == ED_F32) && !h->s.real)
+        return set_error(ED_ERR_INVALID, "ed_position_correlations: real dtype with a complex sector");
+    try {
+        return corr_launch(h->s, dtype, psi_dev, kind, nfixed, fixed_shifts, out_host, (cudaStream_t)stream);
+    } catch (...) {
+        return set_error(ED_ERR_INTERNAL, "ed_position_correlations: exception");
+    }
+}
+
 int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
     if (!h || !counts) return set_error(ED_ERR_INVALID, "ed_sector_row_kinds: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_row_kinds: basis not built");

@@ -184,6 +184,8 @@ int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st);
 int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st);
 int step_free_occupancy(int minb, size_t smem);
 int step_rest_occupancy(size_t smem);
+int corr_launch(const Sector& s, int dtype, const void* psi, int kind, int nfixed, const int* fixed, double* out,
+                cudaStream_t st);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,

@@ -197,6 +197,20 @@ class DeviceSector:
                                                 _ptr(x), _ptr(y), _stream_ptr()))
         return y
 
+    def position_correlations(self, psi: torch.Tensor, kind: str, fixed_shifts=()) -> np.ndarray:
+        """Hole ("hole_correlations") or S^z ("Sz_correlations") correlations of psi over the
+        distances 0..N-1 (ed_position_correlations); fixed_shifts: (leg, rung) pairs."""
+        code = self._code(psi)
+        k = {"hole_correlations": 0, "Sz_correlations": 1}[str(kind)]
+        fixed = np.ascontiguousarray(np.asarray(fixed_shifts, dtype=np.int32).reshape(-1, 2))
+        out = np.zeros(2 * self.key.num_rungs, dtype=np.float64)
+        nat.check("ed_position_correlations",
+                  self._lib.ed_position_correlations(
+                      self._h, code, _ptr(psi), k, len(fixed),
+                      fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if len(fixed) else None,
+                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _stream_ptr()))
+        return out
+
     def normalize(self, x: torch.Tensor, norm_out: torch.Tensor) -> None:
         code = self._code(x)
         nat.check("ed_normalize", self._lib.ed_normalize(self._h, code, _ptr(x), _ptr(norm_out), _stream_ptr()))

@@ -205,5 +205,21 @@ def get_spectral_function_spectra(config: configs.Full_Spectrum_Config, limited_
     return ws, spectra, {"qs_list": qs_list}
 
 
+def get_position_correlations(config: configs.Full_Position_Correlation_Config) -> Spectrum:
+    """Hole or S^z position correlations of the ground state (:104-113)."""
+    from exactdiag_gb300.tJ_spin_half_ladder import position_correlations
+
+    base_name = config.correlations.name
+    if base_name in {"hole_correlations", "Sz_correlations"}:
+        ws, spectrum = position_correlations.get_hole_spin_projection_correlations(config)
+    elif base_name == "singlet-singlet":
+        ws, spectrum = position_correlations.get_singlet_singlet_correlations(config)
+    else:
+        raise ValueError(f"{base_name} is not supported")
+    info = {"fixed_distances": config.correlations.fixed_distances}
+    return Spectrum(ws, spectrum, config, info)
+
+
 __all__ = ["get_eigenpairs", "get_all_k_eigenpairs", "Spectrum", "get_excitation_spectrum", "get_Szq_spectra",
-           "get_spectral_function_spectra", "get_mkx_qxs_qys", "load_calculate_save", "matrix_setup"]
+           "get_spectral_function_spectra", "get_position_correlations", "get_mkx_qxs_qys", "load_calculate_save",
+           "matrix_setup"]

@@ -314,3 +314,109 @@ def _get_spectrum_figure_suffix(hamiltonian_config: Hamiltonian_Config, spectrum
     precision_string = "_mixed" if getattr(hamiltonian_config, "precision", "fp64") == "mixed" else ""
     return (f"{operator_name_suffix}{q_string}{ws_string}{broad_string}{vecs_string}_{weight_string}"
             f"{precision_string}")
+
+
+class Position_Correlation_Name(enum.StrEnum):
+    """Names of the position correlations (:236-241)."""
+
+    HOLE_CORRELATIONS = "hole_correlations"
+    SZ_CORRELATIONS = "Sz_correlations"
+    SINGLET_SINGLET = "singlet-singlet"
+
+
+@dataclasses.dataclass(kw_only=True)
+class Position_Shift:
+    """A relative node position (:244-247, general/configs.py:47-52)."""
+
+    leg: int
+    rung: typing.Literal[0, 1]
+
+    def __post_init__(self):
+        self.leg = int(self.leg)
+        if int(self.rung) not in (0, 1):
+            raise ValueError("rung must be 0 or 1")
+        self.rung = int(self.rung)
+
+    def to_npint32(self):
+        return np.array([self.leg, self.rung], dtype=np.int32)
+
+
+def _shift(value) -> Position_Shift:
+    if isinstance(value, Position_Shift):
+        return value
+    gc._check_fields(Position_Shift, value)
+    return Position_Shift(**value)
+
+
+@dataclasses.dataclass(kw_only=True)
+class Position_Correlation_Part:
+    """Correlation request (:250-275): fixed_distances are the shifts of the fixed number operators
+    relative to the first one (hole and S^z correlations)."""
+
+    name: Position_Correlation_Name
+    fixed_distances: list
+    num_threads: int | None = None
+
+    def __post_init__(self):
+        self.name = Position_Correlation_Name(self.name)
+        self.fixed_distances = [_shift(e) for e in self.fixed_distances]
+
+
+def _correlations(value) -> Position_Correlation_Part:
+    if isinstance(value, Position_Correlation_Part):
+        return value
+    gc._check_fields(Position_Correlation_Part, value)
+    return Position_Correlation_Part(**value)
+
+
+@dataclasses.dataclass(kw_only=True)
+class Limited_Position_Correlation_Config(gc._Json_Loadable):
+    """Hamiltonian plus correlation request (:278-310)."""
+
+    hamiltonian: Hamiltonian_Config
+    correlations: Position_Correlation_Part
+
+    def __post_init__(self):
+        self.hamiltonian = _hamiltonian(self.hamiltonian)
+        self.correlations = _correlations(self.correlations)
+        if self.correlations.num_threads is None:
+            self.correlations.num_threads = self.hamiltonian.num_threads
+
+    def setup_excitation_operator(self, free_shift):
+        """The position-projection operator (:296-310) is the building block of the singlet-singlet
+        correlations, which are not computed by this engine."""
+        raise NotImplementedError("position-correlation operators (singlet-singlet correlations) are not on the GPU path")
+
+
+@dataclasses.dataclass(kw_only=True)
+class Full_Position_Correlation_Config(Limited_Position_Correlation_Config):
+    """Hamiltonian, eigenpair request and correlation request (:313-331)."""
+
+    eigenpair: gc.Eigenpair_Part
+
+    def __post_init__(self):
+        super().__post_init__()
+        if not isinstance(self.eigenpair, gc.Eigenpair_Part):
+            gc._check_fields(gc.Eigenpair_Part, self.eigenpair)
+            self.eigenpair = gc.Eigenpair_Part(**self.eigenpair)
+        if self.eigenpair.num_threads is None:
+            self.eigenpair.num_threads = self.hamiltonian.num_threads
+
+    get_eigenpair_paths = Eigenpair_Config.get_eigenpair_paths
+
+    def get_spectrum_path(self, operator_name_suffix: str = "") -> pathlib.Path:
+        system_folder = self.hamiltonian.get_calc_folder()
+        folder = system_folder / f"{self.correlations.name}_spectra"
+        suffix = _get_position_correlation_figure_suffix(self.hamiltonian, self.correlations, operator_name_suffix)
+        return folder / f"{self.correlations.name}{suffix}.npz"
+
+
+def _get_position_correlation_figure_suffix(hamiltonian_config: Hamiltonian_Config,
+                                            correlation_config: Position_Correlation_Part,
+                                            operator_name_suffix: str) -> str:
+    """(:382-389)"""
+    weight_string = "_".join([f"{name}{weight}" for name, weight in
+                              gc.asdict_shallow(hamiltonian_config.weights).items()])
+    operator_name_suffix = f"_{operator_name_suffix}" if operator_name_suffix else ""
+    fixed_string = f"{[shift.to_npint32().tolist() for shift in correlation_config.fixed_distances]}"
+    return f"{operator_name_suffix}_fixed{fixed_string}_{weight_string}"

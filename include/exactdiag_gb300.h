@@ -152,6 +152,15 @@ int ed_continued_fraction(const double* a_dev, const double* b_dev, int m, const
 int ed_excitation_apply(const ed_sector* src, const ed_sector* dst, int op, int qx, int qy, int initial_sz2, int dtype,
                         const void* x_src_dev, void* y_dst_dev, void* stream);
 
+/* Position correlations of a state psi of the sector (device vector of n entries, dtype as for
+ * ed_hv), distances 0..N-1 written to out_host[N] (host memory; the call synchronises `stream`):
+ *   kind 0, hole correlations: sum_i |psi_i|^2 sum_r [holes at r, rel(r, dist) and every fixed shift of r]
+ *   kind 1, S^z correlations:  the same with the product of the spin signs (0 if any site is a hole)
+ * fixed_shifts holds nfixed (leg, rung) pairs (at most 4), the fixed_distances of the config.
+ * Replaces tJ_spin_half_ladder/position_correlations.pyx:83-118 and :174-207 for one state. */
+int ed_position_correlations(const ed_sector* sector, int dtype, const void* psi_dev, int kind, int nfixed,
+                             const int* fixed_shifts, double* out_host, void* stream);
+
 /* Runs the spectrum Lanczos recursion (general/cython_lanczos_diagonalization.pyx:50-77)
  * for nsec sectors together: m steps each from the start vectors v0_dev[s]
  * (device pointers, dtype, any norm), all sectors' rows handled by one launch per

@@ -334,3 +334,43 @@ def lanczos_dynamical_response(gs, op_apply, h_apply, zs, num_lanczos_vecs):
 
 def num_threads() -> int:
     return int(lib().or_num_threads())
+
+
+def _relative_index(N: int, initial: int, relative: int) -> int:
+    """tJ_spin_half_ladder/symmetry_ladder.h:88-95 get_index_by_relative_index."""
+    initial %= N
+    relative %= N
+    leg = initial // 2 + relative // 2
+    rung = (initial + relative) % 2
+    return (2 * leg + rung) % N
+
+
+def _relative_shift(N: int, initial: int, shift) -> int:
+    """tJ_spin_half_ladder/symmetry_ladder.h:96-101 get_index_by_relative_shift (C++ % on the rung
+    shift, then a positive modulo)."""
+    initial %= N
+    leg = initial // 2 + int(shift[0])
+    r1 = int(shift[1])
+    r1 = r1 - 2 * int(r1 / 2)  # C++ truncating remainder
+    rung = (initial + r1) % 2
+    return (2 * leg + rung) % N
+
+
+def position_correlations(sec: Sector, bas, psi: np.ndarray, name: str, fixed=()) -> np.ndarray:
+    """Hole / S^z correlations of one state over distances 0..N-1
+    (tJ_spin_half_ladder/position_correlations.pyx:83-118, :174-207): every representative's own
+    configuration, weighted by |psi_i|^2, summed over reference sites."""
+    N = sec.N
+    states = np.array([sparse_to_state(sec, s) for s in bas[0]], dtype=np.int16).reshape(-1, N)
+    w = np.abs(np.asarray(psi)) ** 2
+    spin = np.where(states == 1, -1, 1) * (states != 0)  # 0 hole, 1 down, 2 up
+    out = np.zeros(N)
+    for dist in range(N):
+        for r in range(N):
+            pos = [r, _relative_index(N, r, dist)] + [_relative_shift(N, r, f) for f in fixed]
+            if name == "hole_correlations":
+                val = np.all(states[:, pos] == 0, axis=1).astype(float)
+            else:
+                val = np.prod(spin[:, pos], axis=1).astype(float)
+            out[dist] += float(np.dot(w, val))
+    return out

@@ -24,6 +24,12 @@ def reference_fixtures():
 
 
 @pytest.fixture(scope="session")
+def reference_correlations():
+    """The reference's position-correlation fixtures (tests/golden/reference_correlations.json)."""
+    return json.loads((GOLDEN / "reference_correlations.json").read_text())
+
+
+@pytest.fixture(scope="session")
 def golden_sectors():
     return np.load(GOLDEN / "sectors.npz")
 

@@ -15,7 +15,9 @@ Outputs
                            the reference's compiled code, plus 30 spectrum-Lanczos
                            coefficients from the numpy restatement on that matrix;
   excitations.npz          O x for the Szq, spectral_function_minus, spectral_function_plus,
-                           current_rung and current_leg operators.
+                           current_rung and current_leg operators;
+  reference_correlations.json  the reference's position-correlation fixtures
+                           (tests/tJ_spin_half_ladder/precalculated_position_correlations/*.txt).
 """
 
 from __future__ import annotations
@@ -93,6 +95,14 @@ def main() -> None:
         d["file"] = pathlib.Path(f).name
         fixtures.append(d)
     (OUT / "reference_fixtures.json").write_text(json.dumps(fixtures, indent=1))
+
+    corr = []
+    folder = ref_root / "tests" / "tJ_spin_half_ladder" / "precalculated_position_correlations"
+    for f in sorted(folder.glob("*.txt")):
+        for d in json.load(open(f)):
+            d["file"] = f.name
+            corr.append(d)
+    (OUT / "reference_correlations.json").write_text(json.dumps(corr, indent=1))
 
     arrays = {}
     for idx, key in enumerate(SECTORS):

@@ -193,3 +193,18 @@ def test_oracle_excitations_bit_exact_against_reference_code(oracle, name):
                 assert np.max(np.abs(a[2] - b[2]), initial=0) < 1e-14, (key, qx, qy)
                 cases += 1
     assert cases > 0
+
+
+def test_oracle_position_correlation_sum_rules(oracle):
+    """Summed over distances, hole correlations give Nh^2 and S^z correlations (2 S^z)^2 per unit norm."""
+    rng = np.random.default_rng(4)
+    for key in [(4, 2, 3, 0, 0), (5, 1, 4, 1, 1), (4, 0, 3, 1, 0)]:
+        sec = oracle.Sector(*key)
+        bas = oracle.basis(sec)
+        psi = rng.normal(size=len(bas[0])) + 1j * rng.normal(size=len(bas[0]))
+        psi /= np.linalg.norm(psi)
+        holes = oracle.position_correlations(sec, bas, psi, "hole_correlations")
+        spins = oracle.position_correlations(sec, bas, psi, "Sz_correlations")
+        assert abs(holes.sum() - sec.Nh ** 2) < 1e-12
+        assert abs(spins.sum() - sec.Sz2 ** 2) < 1e-12
+        assert abs(holes[0] - sec.Nh) < 1e-12 and abs(spins[0] - (sec.N - sec.Nh)) < 1e-12

@@ -179,6 +179,20 @@ int ed_position_correlations(const ed_sector* h, int dtype, const void* psi_dev,
     }
 }
 
+int ed_singlet_correlations(const ed_sector* h, int dtype, const void* psi_dev, const int fixed_shifts[4],
+                            double* out_host, void* stream) {
+    if (!h || !psi_dev || !out_host || !fixed_shifts)
+        return set_error(ED_ERR_INVALID, "ed_singlet_correlations: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_singlet_correlations: basis not built");
+    if (dtype == ED_F64 && !h->s.real)
+        return set_error(ED_ERR_INVALID, "ed_singlet_correlations: real dtype with a complex sector");
+    try {
+        return singlet_corr_launch(h->s, dtype, psi_dev, fixed_shifts, out_host, (cudaStream_t)stream);
+    } catch (...) {
+        return set_error(ED_ERR_INTERNAL, "ed_singlet_correlations: exception");
+    }
+}
+
 int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
     if (!h || !counts) return set_error(ED_ERR_INVALID, "ed_sector_row_kinds: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_row_kinds: basis not built");

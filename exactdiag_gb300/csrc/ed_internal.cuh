@@ -184,6 +184,7 @@ int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st);
 int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st);
 int step_free_occupancy(int minb, size_t smem);
 int step_rest_occupancy(size_t smem);
+int singlet_corr_launch(const Sector& s, int dtype, const void* psi, const int* fixed, double* out, cudaStream_t st);
 int corr_launch(const Sector& s, int dtype, const void* psi, int kind, int nfixed, const int* fixed, double* out,
                 cudaStream_t st);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,

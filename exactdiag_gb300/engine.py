@@ -211,6 +211,19 @@ class DeviceSector:
                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _stream_ptr()))
         return out
 
+    def singlet_correlations(self, psi: torch.Tensor, fixed_shifts) -> np.ndarray:
+        """Re <psi|O(t)|psi> of the singlet-pair operator for the free shifts t = 0..N-1
+        (ed_singlet_correlations); fixed_shifts: the two (leg, rung) fixed distances."""
+        code = self._code(psi)
+        fixed = np.ascontiguousarray(np.asarray(fixed_shifts, dtype=np.int32).reshape(4))
+        out = np.zeros(2 * self.key.num_rungs, dtype=np.float64)
+        nat.check("ed_singlet_correlations",
+                  self._lib.ed_singlet_correlations(self._h, code, _ptr(psi),
+                                                    fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                    _stream_ptr()))
+        return out
+
     def normalize(self, x: torch.Tensor, norm_out: torch.Tensor) -> None:
         code = self._code(x)
         nat.check("ed_normalize", self._lib.ed_normalize(self._h, code, _ptr(x), _ptr(norm_out), _stream_ptr()))

@@ -161,6 +161,14 @@ int ed_excitation_apply(const ed_sector* src, const ed_sector* dst, int op, int 
 int ed_position_correlations(const ed_sector* sector, int dtype, const void* psi_dev, int kind, int nfixed,
                              const int* fixed_shifts, double* out_host, void* stream);
 
+/* Singlet-singlet correlations of a state psi (dtype ED_F64 or ED_C128): out_host[t] =
+ * Re <psi| O(t) |psi> for t = 0..N-1, O(t) the singlet-pair operator of
+ * tJ_spin_half_ladder/matrix_setup.pyx:434-469 with fixed distances
+ * fixed_shifts = {y leg, y rung, x leg, x rung} and free shift (t / 2, t % 2), columns by the
+ * reference's column rule.  Replaces position_correlations.pyx:112-124 for one state. */
+int ed_singlet_correlations(const ed_sector* sector, int dtype, const void* psi_dev, const int fixed_shifts[4],
+                            double* out_host, void* stream);
+
 /* Runs the spectrum Lanczos recursion (general/cython_lanczos_diagonalization.pyx:50-77)
  * for nsec sectors together: m steps each from the start vectors v0_dev[s]
  * (device pointers, dtype, any norm), all sectors' rows handled by one launch per

@@ -395,7 +395,7 @@ int or_orbit_lowest(int L, int Nh, int Nd, int kx, int ky, const int16_t *state,
 typedef struct {
     int n;                   /* number of operator index combinations */
     int len;                 /* indices per combination (1 or 2) */
-    int16_t idx[2 * OR_MAXN][2];
+    int16_t idx[2 * OR_MAXN][4];
     double complex wd[2 * OR_MAXN], wo[2 * OR_MAXN];
 } combos_t;
 
@@ -515,18 +515,27 @@ typedef enum {
     VAL_ALL_DOWN = 3,  /* :39-44 */
     VAL_ALL_UP = 4,    /* :32-37 */
     VAL_ALL_HOLES = 5, /* :46-51 */
+    VAL_UNEQUAL_SPINS_2HOLES = 6, /* :53-62 */
 } validator_t;
 
 /* tJ_spin_half_ladder/matrix_element_functions.pyx: swap, dont_change, add_hole (:112-118),
  * add_spin_down (:98-103), add_spin_up (:105-110) */
-typedef enum { NEW_SWAP = 0, NEW_KEEP = 1, NEW_ADD_HOLE = 2, NEW_ADD_DOWN = 3, NEW_ADD_UP = 4 } newstate_t;
+typedef enum {
+    NEW_SWAP = 0,
+    NEW_KEEP = 1,
+    NEW_ADD_HOLE = 2,
+    NEW_ADD_DOWN = 3,
+    NEW_ADD_UP = 4,
+    NEW_REMOVE_TWO_ADD_UP_DOWN = 5, /* :120-130 */
+} newstate_t;
 
 typedef struct {
     const combos_t *c;
     validator_t valid;
     newstate_t gen;
     int use_sign;        /* get_anticommutation_sign */
-    int spin_weights;    /* get_weights_spin_projection (matrix_element_functions.pyx:71-82) */
+    int spin_weights;    /* 1: get_weights_spin_projection (matrix_element_functions.pyx:71-82);
+                          * 2: get_weights_annihilation_part_singlet_singlet (:84-95) */
     int triangle;        /* is_valid_indices_triangular (column_functions.h:71-73) */
     const ors_t *fin;    /* final-sector translator */
     const int64_t *fin_d2s;
@@ -549,6 +558,13 @@ static int is_valid(validator_t v, const st_t *st, const int16_t *ind, int len) 
         for (int i = 0; i < len; ++i)
             if (st[ind[i]] != HOLE) return 0;
         return 1;
+    case VAL_UNEQUAL_SPINS_2HOLES: {
+        if (ind[0] == ind[1]) return 0;
+        const int h0 = ind[0] == ind[2] || ind[0] == ind[3] || st[ind[0]] == HOLE;
+        const int h1 = ind[1] == ind[2] || ind[1] == ind[3] || st[ind[1]] == HOLE;
+        const int sp = st[ind[2]] != st[ind[3]] && st[ind[2]] != HOLE && st[ind[3]] != HOLE;
+        return h0 && h1 && sp;
+    }
     default:
         for (int i = 0; i < len; ++i)
             if (st[ind[i]] != UP) return 0;
@@ -570,12 +586,15 @@ static int column(const ors_t *ini, int64_t col, int64_t sparse, int orbit_size,
         const int16_t *ind = r->c->idx[k];
         double complex ed = diag_w * r->c->wd[k], eo = off_w * r->c->wo[k];
         if (!is_valid(r->valid, st, ind, r->c->len)) continue;
-        if (r->spin_weights) {
+        if (r->spin_weights == 1) {
             double f = 1.0;
             for (int i = 0; i < r->c->len; ++i)
                 if (st[ind[i]] == DOWN) f *= -1.0;
             ed *= f;
             eo *= f;
+        } else if (r->spin_weights == 2 && st[ind[2]] == DOWN) {
+            ed *= -1.0;
+            eo *= -1.0;
         }
         if (cabs(ed) > 1e-8) add_elem(ed, col, vals, inds, &n);
         if (cabs(eo) < 1e-8) continue;
@@ -586,6 +605,10 @@ static int column(const ors_t *ini, int64_t col, int64_t sparse, int orbit_size,
         } else if (r->gen == NEW_ADD_HOLE || r->gen == NEW_ADD_DOWN || r->gen == NEW_ADD_UP) {
             const st_t v = r->gen == NEW_ADD_HOLE ? HOLE : (r->gen == NEW_ADD_DOWN ? DOWN : UP);
             for (int i = 0; i < r->c->len; ++i) ns[ind[i]] = v;
+        } else if (r->gen == NEW_REMOVE_TWO_ADD_UP_DOWN) {
+            /* the last index acts first: holes at 3 and 2, then up at 1, down at 0 (repeating) */
+            static const st_t changes[4] = {HOLE, HOLE, UP, DOWN};
+            for (int i = 0; i < r->c->len; ++i) ns[ind[r->c->len - 1 - i]] = changes[i % 4];
         }
         int64_t fs;
         double complex amp;
@@ -741,6 +764,38 @@ int or_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz2
     } else {
         return OR_EINVAL;
     }
+    return rule_columns(&s, d2s, orb, n, &r, colptr, rows, vre, vim, cap, nnz_out);
+}
+
+/* Singlet-singlet position-correlation operator (tJ_spin_half_ladder/matrix_setup.pyx:434-469):
+ * startpoints i, endpoint shift sets (f0, fs, f1 + fs) and (-f0, fs - f0, f1 + fs - f0) with
+ * f0, f1 the fixed distances and fs the free shift (each (leg, rung)), reverse=False; weights
+ * (0, 0.5/N); validator is_valid_state_unequal_spins_2holes, remove_two_add_up_down,
+ * get_weights_annihilation_part_singlet_singlet and the anticommutation sign.  Same sector in and
+ * out.  shifts = {f0 leg, f0 rung, f1 leg, f1 rung, fs leg, fs rung}. */
+int or_singlet_columns(int L, int Nh, int Nd, int kx, int ky, const int64_t *d2s, const int32_t *orb, int64_t n,
+                       const int *shifts, int64_t *colptr, int64_t *rows, double *vre, double *vim, int64_t cap,
+                       int64_t *nnz_out) {
+    ors_t s;
+    if (sector_init(&s, L, Nh, Nd, kx, ky) != OR_OK || !shifts) return OR_EINVAL;
+    const int f0[2] = {shifts[0], shifts[1]}, f1[2] = {shifts[2], shifts[3]}, fs[2] = {shifts[4], shifts[5]};
+    const int sets[2][3][2] = {
+        {{f0[0], f0[1]}, {fs[0], fs[1]}, {f1[0] + fs[0], f1[1] + fs[1]}},
+        {{-f0[0], -f0[1]}, {fs[0] - f0[0], fs[1] - f0[1]}, {f1[0] + fs[0] - f0[0], f1[1] + fs[1] - f0[1]}},
+    };
+    combos_t c;
+    c.n = 0;
+    c.len = 4;
+    for (int first = 0; first < s.N; ++first)
+        for (int e = 0; e < 2; ++e) {
+            c.idx[c.n][0] = (int16_t)first;
+            for (int k = 0; k < 3; ++k)
+                c.idx[c.n][k + 1] = (int16_t)index_by_relative_shift(s.N, first, sets[e][k][0], sets[e][k][1]);
+            c.wd[c.n] = 0.0;
+            c.wo[c.n] = 0.5 / (double)s.N;
+            c.n++;
+        }
+    rule_t r = {&c, VAL_UNEQUAL_SPINS_2HOLES, NEW_REMOVE_TWO_ADD_UP_DOWN, 1, 2, 0, &s, d2s, n};
     return rule_columns(&s, d2s, orb, n, &r, colptr, rows, vre, vim, cap, nnz_out);
 }
 

@@ -374,3 +374,31 @@ def position_correlations(sec: Sector, bas, psi: np.ndarray, name: str, fixed=()
                 val = np.prod(spin[:, pos], axis=1).astype(float)
             out[dist] += float(np.dot(w, val))
     return out
+
+
+def singlet_columns(sec: Sector, bas, shifts, impl: str = "oracle"):
+    """Column-major singlet-singlet correlation operator for one free shift
+    (tJ_spin_half_ladder/matrix_setup.pyx:434-469); shifts = (f0, f1, free), each (leg, rung)."""
+    sp, orb = bas
+    sh = np.ascontiguousarray(np.asarray(shifts, dtype=np.int32).reshape(6))
+    shp = sh.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    if impl == "ref":
+        r = ref_lib()
+        if r is None:
+            raise RuntimeError("oracle/_ref is not built")
+        args = (*sec.args(), _p(sp, _i64p), _p(orb, _i32p), ctypes.c_int64(len(sp)), shp)
+        return _columns(r.ref_singlet_columns, args, len(sp), "ref singlet")
+    args = (*sec.args(), _p(sp, _i64p), _p(orb, _i32p), ctypes.c_int64(len(sp)), shp)
+    return _columns(lib().or_singlet_columns, args, len(sp), "oracle singlet")
+
+
+def singlet_correlations(sec: Sector, bas, gs: np.ndarray, fixed) -> np.ndarray:
+    """Re <gs| O(free) |gs> for the free shifts of every distance index, free = (d // 2, d % 2)
+    (tJ_spin_half_ladder/position_correlations.pyx:112-124)."""
+    n = len(bas[0])
+    out = np.zeros(sec.N)
+    for d in range(sec.N):
+        colptr, rows, vals = singlet_columns(sec, bas, [fixed[0], fixed[1], (d // 2, d % 2)])
+        op = _csc(colptr, rows, vals, (n, n))
+        out[d] = float(np.real(np.vdot(gs, op @ gs)))
+    return out

@@ -87,6 +87,29 @@ bool valid_all_holes(const state_int* s, const pos_int* ind, int len) {
         if (s[ind[i]] != HOLE_VALUE) return false;
     return true;
 }
+bool valid_unequal_spins_2holes(const state_int* s, const pos_int* ind, int) {
+    if (ind[0] == ind[1]) return false;
+    bool h0 = ind[0] == ind[2] || ind[0] == ind[3] || s[ind[0]] == HOLE_VALUE;
+    bool h1 = ind[1] == ind[2] || ind[1] == ind[3] || s[ind[1]] == HOLE_VALUE;
+    bool sp = s[ind[2]] != s[ind[3]] && s[ind[2]] != HOLE_VALUE && s[ind[3]] != HOLE_VALUE;
+    return h0 && h1 && sp;
+}
+// matrix_element_functions.pyx:84-95
+void weights_singlet_annihilation(const state_int* s, const vector<pos_int>& ind, VALUE_TYPE& ed, VALUE_TYPE& eo) {
+    VALUE_TYPE f = s[ind[2]] == SPIN_DOWN_VALUE ? -1 : 1;
+    ed *= f;
+    eo *= f;
+}
+// matrix_element_functions.pyx:120-130
+void remove_two_add_up_down(const state_int* in, state_int* out, pos_int n, const vector<pos_int>& ind) {
+    static const state_int changes[4] = {HOLE_VALUE, HOLE_VALUE, SPIN_UP_VALUE, SPIN_DOWN_VALUE};
+    memcpy(out, in, n * sizeof(state_int));
+    int rem = 0, len = (int)ind.size();
+    for (int i = 0; i < len; ++i) {
+        out[ind[len - 1 - i]] = changes[rem];
+        rem += 1 - 4 * (rem / 3);
+    }
+}
 // matrix_element_functions.pyx:66-69 -> general/column_functions.h:317 count_commutations.
 int anticommutation_sign(const state_int* s, pos_int n, const vector<pos_int>& ind) {
     int count = count_commutations(s, n, ind, HOLE_VALUE, false);
@@ -287,6 +310,39 @@ int ref_excitation_columns(int op, int L, int Nh, int Nd, int kx, int ky, int Sz
             return -1;
         }
         Lambda_Column colf(imap, s.trans, el, true);
+        return run_columns(colf, n, colptr, rows, vre, vim, cap, nnz_out, (int)idx.size() + 2);
+    } catch (...) {
+        return -1;
+    }
+}
+
+// tJ_spin_half_ladder/matrix_setup.pyx:434-469: the singlet-singlet correlation operator for one
+// free shift; shifts = {f0 leg, f0 rung, f1 leg, f1 rung, free leg, free rung}.
+int ref_singlet_columns(int L, int Nh, int Nd, int kx, int ky, const int64_t* d2s, const int32_t* orb, int64_t n,
+                        const int* shifts, int64_t* colptr, int64_t* rows, double* vre, double* vim, int64_t cap,
+                        int64_t* nnz_out) {
+    try {
+        Sector s(L, Nh, Nd, kx, ky);
+        auto bmap = make_map(d2s, orb, n);
+        int N = 2 * L;
+        int f0[2] = {shifts[0], shifts[1]}, f1[2] = {shifts[2], shifts[3]}, fs[2] = {shifts[4], shifts[5]};
+        int sets[2][3][2] = {{{f0[0], f0[1]}, {fs[0], fs[1]}, {f1[0] + fs[0], f1[1] + fs[1]}},
+                             {{-f0[0], -f0[1]}, {fs[0] - f0[0], fs[1] - f0[1]},
+                              {f1[0] + fs[0] - f0[0], f1[1] + fs[1] - f0[1]}}};
+        vector<vector<pos_int>> idx;
+        vector<vector<VALUE_TYPE>> w;
+        // general/matrix_rules_utils.pyx:15-87, reverse=False, weights (0, 0.5/N) x (0, 1)
+        for (int first = 0; first < N; ++first)
+            for (int e = 0; e < 2; ++e) {
+                vector<pos_int> c{(pos_int)first};
+                for (int k = 0; k < 3; ++k) c.push_back(s.sym->get_index_by_relative_shift(first, sets[e][k]));
+                idx.push_back(c);
+                w.push_back({0.0, 0.5 / (double)N});
+            }
+        auto el = std::shared_ptr<I_Lambda_Matrix_Elements>(new Lambda_Matrix_Elements(
+            s.trans, bmap, N, remove_two_add_up_down, valid_unequal_spins_2holes, nullptr,
+            weights_singlet_annihilation, anticommutation_sign, idx, w));
+        Lambda_Column colf(bmap, s.trans, el, true);
         return run_columns(colf, n, colptr, rows, vre, vim, cap, nnz_out, (int)idx.size() + 2);
     } catch (...) {
         return -1;

@@ -47,3 +47,41 @@ def test_hole_correlations_match_reference_fixtures(cuda, reference_correlations
         assert np.all(np.abs(diff) < 1e-3), (d["hamiltonian"], diff)
         checked += 1
     assert checked == 16
+
+
+@pytest.mark.parametrize("key", [(5, 2, 4, 0, 0), (6, 4, 4, 0, 0), (5, 3, 3, 2, 1), (6, 2, 5, 1, 0)])
+@pytest.mark.parametrize("fixed", [((1, 1), (1, 1)), ((1, 0), (0, 1)), ((0, 1), (1, 0))])
+def test_singlet_correlations_vs_oracle(cuda, oracle, key, fixed):
+    torch = cuda
+    from exactdiag_gb300.engine import DeviceSector
+
+    sec = DeviceSector(*key)
+    osec = oracle.Sector(*key)
+    bas = oracle.basis(osec)
+    psi = seeded_vector(len(bas[0]), 13, not sec.is_real)
+    if sec.is_real:
+        psi = psi.real
+    psi = psi / np.linalg.norm(psi)
+    want = oracle.singlet_correlations(osec, bas, psi.astype(np.complex128), fixed)
+    got = sec.singlet_correlations(torch.as_tensor(psi, device=sec.device), fixed)
+    assert np.max(np.abs(got - want)) < 1e-12
+
+
+def test_singlet_correlations_match_reference_fixtures(cuda, reference_correlations, in_tmp):
+    """The reference's published singlet-singlet correlations (its test_position_correlations.py),
+    unnormalised, to the listed precision 1e-3."""
+    from exactdiag_gb300.tJ_spin_half_ladder import api
+    from exactdiag_gb300.tJ_spin_half_ladder import configs as lc
+
+    checked = 0
+    for d in reference_correlations:
+        if d["correlations"]["name"] != "singlet-singlet":
+            continue
+        d = {k: v for k, v in d.items() if k != "file"}
+        target = d.pop("probabilities")
+        config = lc.Full_Position_Correlation_Config(**d)
+        values = api.get_position_correlations(config).spectrum.flatten()
+        diff = values[: len(target)] - np.asarray(target)
+        assert np.all(np.abs(diff) < 1e-3), (d["hamiltonian"]["weights"], d["correlations"], diff)
+        checked += 1
+    assert checked == 18

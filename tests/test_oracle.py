@@ -208,3 +208,18 @@ def test_oracle_position_correlation_sum_rules(oracle):
         assert abs(holes.sum() - sec.Nh ** 2) < 1e-12
         assert abs(spins.sum() - sec.Sz2 ** 2) < 1e-12
         assert abs(holes[0] - sec.Nh) < 1e-12 and abs(spins[0] - (sec.N - sec.Nh)) < 1e-12
+
+
+def test_oracle_singlet_operator_bit_exact_against_reference_code(oracle):
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference's code is not built here")
+    for key in [(5, 2, 4, 0, 0), (6, 4, 4, 0, 0), (5, 3, 3, 2, 1), (6, 2, 5, 1, 0)]:
+        sec = oracle.Sector(*key)
+        bas = oracle.basis(sec)
+        for fixed in [((1, 1), (1, 1)), ((1, 0), (0, 1)), ((0, 1), (1, 0))]:
+            for d in range(sec.N):
+                shifts = [fixed[0], fixed[1], (d // 2, d % 2)]
+                a = oracle.singlet_columns(sec, bas, shifts)
+                b = oracle.singlet_columns(sec, bas, shifts, impl="ref")
+                assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (key, fixed, d)
+                assert np.max(np.abs(a[2] - b[2]), initial=0) < 1e-14, (key, fixed, d)

@@ -112,6 +112,9 @@ int build_descriptors(Sector& s) {
         D.ncand = (uint8_t)std::min(nst, kMaxCand);
         D.mode = (nst == 1) ? kModeFree : (nst <= kMaxCand ? kModeCand : kModeGeneric);
         if (S.Nh > 4) D.mode = kModeGeneric;
+        // the fast rows take the first stabiliser candidate to be the identity (its image is the state)
+        if (D.mode == kModeCand && (D.cand[0].p != 0 || D.cand[0].swap != 0 || D.cand[0].rot != 0))
+            D.mode = kModeGeneric;
         if (D.mode == kModeGeneric) {
             desc[b] = D;
             continue;

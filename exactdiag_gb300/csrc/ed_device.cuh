@@ -284,14 +284,22 @@ __device__ __forceinline__ uint32_t cand_image(const CandParams& c, uint32_t x, 
 // reaching it (the state's stabiliser order: orbit = 2L / count) and its phase; the state is
 // incompatible with the sector when those candidates disagree in phase (the reference's
 // amplitude tests, symmetry_ladder.h:196-224).
+// Orbit size 2L / count of a state whose lowest image `count` coset candidates reach (count <= 4):
+// shifts and a multiply in place of an integer division.
+__device__ __forceinline__ int orbit_of_count(int N, int count) {
+    return count == 1 ? N : (count == 2 ? (N >> 1) : (count == 4 ? (N >> 2) : ((N * 21846) >> 16)));
+}
+
 struct CandResult {
     uint32_t best;
     int count, e;
     bool valid;
 };
 
+// FIRST_IDENTITY: c[0] is the identity (a block's own stabiliser lists it first), so its image is x.
+template <bool FIRST_IDENTITY = false>
 __device__ __forceinline__ CandResult resolve_cand(const CandParams* c, int nc, uint32_t x, int Ns) {
-    CandResult r{cand_image(c[0], x, Ns), 1, c[0].e, true};
+    CandResult r{FIRST_IDENTITY ? x : cand_image(c[0], x, Ns), 1, c[0].e, true};
     for (int k = 1; k < nc; ++k) {
         const uint32_t img = cand_image(c[k], x, Ns);
         if (img < r.best) {
@@ -348,20 +356,20 @@ __device__ __forceinline__ void gather4(const void* __restrict__ x, const int64_
     }
 }
 
-// Four gathers from one block: x_blk points at the block's first row, offsets are 32-bit rows
+// K gathers from one block: x_blk points at the block's first row, offsets are 32-bit rows
 // inside it; slots whose bit in `live` is clear contribute nothing.
-template <typename R, bool CPLX>
-__device__ __forceinline__ void gather4_block(const typename Vec<R, CPLX>::T* __restrict__ xb,
-                                              const uint32_t (&off)[4], unsigned live, const R (&c)[4],
-                                              R& accr, R& acci) {
-    R xr[4], xi[4];
+template <typename R, bool CPLX, int K>
+__device__ __forceinline__ void gather_block(const typename Vec<R, CPLX>::T* __restrict__ xb,
+                                             const uint32_t (&off)[K], unsigned live, const R (&c)[K],
+                                             R& accr, R& acci) {
+    R xr[K], xi[K];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < K; ++u) {
         if ((live >> u) & 1u) ld<R, CPLX>(xb, off[u], xr[u], xi[u]);
         else xr[u] = xi[u] = R(0);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < K; ++u) {
         accr += c[u] * xr[u];
         if constexpr (CPLX) acci += c[u] * xi[u];
     }
@@ -409,13 +417,15 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         const R cr = R(0.5) * wr, cl = R(0.5) * wl;
         const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(x) + dstart;
         const uint32_t ri = (uint32_t)(i - dstart);
-        uint32_t off[4];
-        R cb[4];
+        // exchange targets gathered kExBatch at a time (loads in flight per thread)
+        constexpr int kExBatch = 4;
+        uint32_t off[kExBatch];
+        R cb[kExBatch];
         uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
         while (m1) {
             unsigned live = 0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kExBatch; ++u) {
                 off[u] = ri;
                 cb[u] = R(0);
                 if (m1) {
@@ -428,13 +438,13 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                     live |= 1u << u;
                 }
             }
-            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
+            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
         }
         uint32_t mm = cl != R(0) ? m2 : 0u;
         while (mm) {
             unsigned live = 0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kExBatch; ++u) {
                 off[u] = ri;
                 cb[u] = R(0);
                 if (mm) {
@@ -448,12 +458,12 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                     live |= 1u << u;
                 }
             }
-            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
+            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
         }
         if (cl != R(0) && wrap_anti) {
             unsigned live = 0;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kExBatch; ++u) {
                 off[u] = ri;
                 cb[u] = R(0);
                 if (u < 2 && ((wrap_anti >> u) & 1u)) {
@@ -463,7 +473,7 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                     live |= 1u << u;
                 }
             }
-            gather4_block<R, CPLX>(xb, off, live, cb, accr, acci);
+            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
         }
     } else {
         // non-free block: each exchange target is resolved through the block's stabiliser (lowest
@@ -486,11 +496,11 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                 m &= m - 1u;
                 const uint32_t flip = dist ? ((1u << a) | (1u << (a + dist)))
                                            : ((1u << (a ? wlo[1] : wlo[0])) | (1u << (a ? whi[1] : whi[0])));
-                const CandResult cr2 = resolve_cand(D->cand, ncand, dc ^ flip, Ns);
+                const CandResult cr2 = resolve_cand<true>(D->cand, ncand, dc ^ flip, Ns);
                 if (!cr2.valid) continue;
                 const int64_t j = bitmap_row(S, word_off, spin_rank(cr2.best, tb.rank, S.Nd));
                 if (j < 0) continue;
-                gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[N / cr2.count], cr2.e, tb, accr, acci);
+                gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[orbit_of_count(N, cr2.count)], cr2.e, tb, accr, acci);
             }
         }
     }
@@ -535,7 +545,7 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                     bitmap_row(S, (int64_t)(((uint64_t)hw1.w << 32) | hw1.z), spin_rank(cr2.best, tb.rank, S.Nd));
                 if (j < 0) continue;
                 jj[u] = j;
-                cc[u] = coef * tb.rsqrtv[N / cr2.count];
+                cc[u] = coef * tb.rsqrtv[orbit_of_count(N, cr2.count)];
                 ee[u] = cr2.e;
             }
         }

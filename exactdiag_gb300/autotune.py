@@ -82,6 +82,26 @@ def step_launches(sector: DeviceSector) -> int:
     return sum(1 for c in row_kinds(sector) if c > 0) + 1 + 4
 
 
+_MEMO: dict = {}
+MIN_ROWS = 1 << 20  # smaller sectors keep the default launch: their steps take microseconds
+
+
+def ensure(sector: DeviceSector, weights, dtype: torch.dtype) -> dict | None:
+    """Apply the tuned launch for this sector shape and dtype: from this process's memo, else the
+    JSON cache, else by timing the candidates once.  Sectors below MIN_ROWS rows, or with
+    EXACTDIAG_GB300_NO_TUNE=1 set, keep the default launch (3 CTAs per SM, all that fit)."""
+    if sector.n < MIN_ROWS or os.environ.get("EXACTDIAG_GB300_NO_TUNE") == "1":
+        return None
+    key = _key(sector, dtype)
+    rec = _MEMO.get(key)
+    if rec is None:
+        rec = tune(sector, weights, dtype)
+        _MEMO[key] = rec
+    else:
+        set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+    return rec
+
+
 def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_cache: bool = True) -> dict:
     """Apply the fastest launch configuration for this sector shape; returns the record used."""
     key = _key(sector, dtype)

@@ -234,10 +234,13 @@ def batch_lanczos(sectors: list, weights, v0s: list, num_lanczos_vecs: int, use_
 
     Returns one (a, b, |v0|) per sector, truncated like _lanczos_get_anbn.
     """
+    from exactdiag_gb300 import autotune
+
     lib = nat.load()
     m = int(num_lanczos_vecs)
     nsec = len(sectors)
     stride = 2 * m + 4
+    autotune.ensure(sectors[0], weights, v0s[0].dtype)  # the batch runs with the first sector's launch
     dev = sectors[0].device
     coef = torch.zeros(nsec * stride, dtype=torch.float64, device=dev)
     code = _CODE_OF_TORCH[v0s[0].dtype]

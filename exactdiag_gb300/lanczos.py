@@ -34,6 +34,9 @@ class LanczosRun:
         self.scal = torch.zeros(2 * self.m + 4, dtype=torch.float64, device=dev)
         self.norm = torch.zeros(1, dtype=torch.float64, device=dev)
         self.graph = None
+        from exactdiag_gb300 import autotune
+
+        autotune.ensure(sector, self.weights, dtype)
 
     def _record(self, ritz=None, acc=None) -> None:
         s = self.sector

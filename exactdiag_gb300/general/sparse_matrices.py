@@ -77,3 +77,76 @@ class Device_Operator:
         dt = torch.complex128 if self.precision == "fp64" else torch.complex64
         x = torch.as_tensor(v).to(device=self.src.device, dtype=dt)
         return self.device_dot(x).cpu().numpy().astype(VALUE_TYPE)
+
+
+TERMS = ("tl", "tr", "jl", "jr")
+
+
+class Sparse_Matrix:
+    """One Hamiltonian term of a sector (general/sparse_matrices.py:27-139), applied matrix-free.
+
+    The reference loads the term's stored matrix from the sector's calculation folder; here
+    from_name gives the same `.dot(vec, weight=1, matvec=None)` / `.shape` / `.toarray` protocol
+    over the GPU operator with that term's weight set to one.
+    """
+
+    def __init__(self, sector: DeviceSector, name: str, num_threads: int = 1, precision: str = "fp64"):
+        if name not in TERMS:
+            raise ValueError(f"unknown Hamiltonian term {name!r}; expected one of {TERMS}")
+        self.name = name
+        self.num_threads = num_threads
+        self._op = Device_Hamiltonian(sector, {t: (1.0 if t == name else 0.0) for t in TERMS}, num_threads,
+                                      precision)
+        self.shape = self._op.shape
+
+    @classmethod
+    def from_name(cls, name: str, config, num_threads: int | None = None) -> "Sparse_Matrix":
+        """The term `name` of the sector `config` (a Hamiltonian config) describes (:127-139)."""
+        from exactdiag_gb300.tJ_spin_half_ladder.matrix_setup import sector_of
+
+        num_threads = config.num_threads if num_threads is None else num_threads
+        return cls(sector_of(config), name, num_threads, getattr(config, "precision", "fp64"))
+
+    def dot(self, vec, weight=1, matvec=None) -> np.ndarray:
+        """matvec + weight * (term @ vec) (the reference's accumulate-into convention)."""
+        out = complex(weight) * self._op.dot(vec)
+        return out if matvec is None else matvec + out
+
+    def toarray(self) -> np.ndarray:
+        return self._op.toarray()
+
+
+class Added_Sparse_Matrices:
+    """Weighted sum of operators with a common shape (general/sparse_matrices.py:210-243)."""
+
+    def __init__(self, mats, weights=None):
+        self.refs = list(mats)
+        if any(m.shape != self.refs[0].shape for m in self.refs[1:]):
+            raise ValueError("incompatible shapes")
+        self.shape = self.refs[0].shape
+        self.num_matrices = len(self.refs)
+        if weights is None:
+            weights = [1] * self.num_matrices
+        elif len(weights) != self.num_matrices:
+            raise ValueError("wrong weights supplied")
+        self.weights = np.array(list(weights), dtype=VALUE_TYPE)
+        self.num_threads = max(getattr(m, "num_threads", 1) for m in self.refs)
+
+    def add_matrix(self, matrix, weight) -> None:
+        if self.shape != matrix.shape:
+            raise ValueError(f"Nonmatching shapes {self.shape} and {matrix.shape}.")
+        self.refs.append(matrix)
+        self.weights = np.append(self.weights, VALUE_TYPE(weight))
+        self.num_matrices += 1
+
+    def dot(self, vec) -> np.ndarray:
+        matvec = None
+        for m, w in zip(self.refs, self.weights):
+            matvec = m.dot(vec, w, matvec)
+        return matvec
+
+    def toarray(self) -> np.ndarray:
+        mat = np.zeros(self.shape, dtype=VALUE_TYPE)
+        for m, w in zip(self.refs, self.weights):
+            mat += w * m.toarray()
+        return mat

@@ -220,6 +220,39 @@ def get_position_correlations(config: configs.Full_Position_Correlation_Config) 
     return Spectrum(ws, spectrum, config, info)
 
 
+def _plot(name: str, spectrum: Spectrum, show: bool) -> None:
+    """A plain figure of a computed spectrum or correlation when matplotlib is installed; the
+    reference's styled figures (plotting.py) are not part of this package."""
+    try:
+        import matplotlib.pyplot as plt
+    except ImportError:
+        return
+    data = np.asarray(spectrum.spectrum)
+    fig, ax = plt.subplots()
+    if data.ndim == 1:
+        ax.plot(data)
+    else:
+        ax.imshow(data.reshape(-1, data.shape[-1]), aspect="auto", origin="lower")
+    ax.set_title(str(name))
+    if show:
+        plt.show()
+
+
+def plot_excitation_spectrum(config: configs.Full_Spectrum_Config, show: bool = False, **kwargs) -> Spectrum:
+    """Compute the spectra get_excitation_spectrum gives (:202-204) and draw them if matplotlib is
+    installed; returns the Spectrum."""
+    spectrum = get_excitation_spectrum(config=config, **kwargs)
+    _plot(config.spectrum.name, spectrum, show)
+    return spectrum
+
+
+def plot_position_correlation(config: configs.Full_Position_Correlation_Config, show: bool = False) -> Spectrum:
+    """Compute the position correlations (:207-209) and draw them if matplotlib is installed."""
+    spectrum = get_position_correlations(config=config)
+    _plot(config.correlations.name, spectrum, show)
+    return spectrum
+
+
 __all__ = ["get_eigenpairs", "get_all_k_eigenpairs", "Spectrum", "get_excitation_spectrum", "get_Szq_spectra",
-           "get_spectral_function_spectra", "get_position_correlations", "get_mkx_qxs_qys", "load_calculate_save",
-           "matrix_setup"]
+           "get_spectral_function_spectra", "get_position_correlations", "plot_excitation_spectrum",
+           "plot_position_correlation", "get_mkx_qxs_qys", "load_calculate_save", "matrix_setup"]

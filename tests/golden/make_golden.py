@@ -17,7 +17,8 @@ Outputs
   excitations.npz          O x for the Szq, spectral_function_minus, spectral_function_plus,
                            current_rung and current_leg operators;
   reference_correlations.json  the reference's position-correlation fixtures
-                           (tests/tJ_spin_half_ladder/precalculated_position_correlations/*.txt).
+                           (tests/tJ_spin_half_ladder/precalculated_position_correlations/*.txt);
+  reference_examples.json  the configurations of examples/tJ_spin_half_ladder/*.json.
 """
 
 from __future__ import annotations
@@ -103,6 +104,12 @@ def main() -> None:
             d["file"] = f.name
             corr.append(d)
     (OUT / "reference_correlations.json").write_text(json.dumps(corr, indent=1))
+
+    # the example configurations (examples/tJ_spin_half_ladder/*.json) for the drop-in test
+    examples = {}
+    for f in sorted((ref_root / "examples" / "tJ_spin_half_ladder").glob("*.json")):
+        examples[f.stem] = json.load(open(f))
+    (OUT / "reference_examples.json").write_text(json.dumps(examples, indent=1))
 
     arrays = {}
     for idx, key in enumerate(SECTORS):

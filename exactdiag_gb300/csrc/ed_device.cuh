@@ -586,21 +586,6 @@ __device__ __forceinline__ void stage_block(const BlockDesc* __restrict__ src, B
     __syncthreads();
 }
 
-// Stage the block descriptor of row `first` in shared memory (all threads of the CTA call this).
-__device__ __forceinline__ const BlockDesc* stage_desc(const SectorView& S, const uint32_t* comb, int64_t first,
-                                                       BlockDesc* sdesc) {
-    if (S.desc == nullptr) return nullptr;
-    __syncthreads();  // the previous chunk's rows are done with sdesc
-    const uint32_t h = (uint32_t)(S.keys[first] >> 32);
-    const BlockDesc* src = S.desc + S.holes[hole_rank(h, comb)].block;
-    const int words = (int)(sizeof(BlockDesc) / sizeof(uint32_t));
-    const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
-    uint32_t* d32 = reinterpret_cast<uint32_t*>(sdesc);
-    for (int t = threadIdx.x; t < words; t += blockDim.x) d32[t] = s32[t];
-    __syncthreads();
-    return sdesc;
-}
-
 template <typename R>
 __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
     uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem);

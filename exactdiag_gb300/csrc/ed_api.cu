@@ -234,21 +234,25 @@ static bool weights_ok(const double* w, HvWeights& out) {
 }
 
 int ed_hv(const ed_sector* h, const double weights[4], int dtype, const void* x_dev, void* y_dev, void* stream) {
-    if (!h || !x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv: NULL argument");
+    if (!h) return set_error(ED_ERR_INVALID, "ed_hv: NULL sector");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_hv: basis not built");
     HvWeights w;
     if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_hv: weights");
+    if (h->s.view.n == 0) return ED_OK;  // empty sector: nothing to read or write (the vectors may be NULL)
+    if (!x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv: NULL argument");
     if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv: x and y must not alias");
     return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
 }
 
 int ed_hv_mode(const ed_sector* h, const double weights[4], int dtype, const void* x_dev, void* y_dev, int mode,
                void* stream) {
-    if (!h || !x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv_mode: NULL argument");
+    if (!h) return set_error(ED_ERR_INVALID, "ed_hv_mode: NULL sector");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_hv_mode: basis not built");
     if (mode != 0 && mode != 1) return set_error(ED_ERR_INVALID, "ed_hv_mode: mode must be 0 or 1");
     HvWeights w;
     if (!weights_ok(weights, w)) return set_error(ED_ERR_INVALID, "ed_hv_mode: weights");
+    if (h->s.view.n == 0) return ED_OK;
+    if (!x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv_mode: NULL argument");
     if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv_mode: x and y must not alias");
     w.faithful = mode;
     return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
@@ -256,6 +260,7 @@ int ed_hv_mode(const ed_sector* h, const double weights[4], int dtype, const voi
 
 int ed_lanczos_step(const ed_sector* h, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
                     void* v_next_dev, double* scal_dev, void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_lanczos_step: empty sector");
     if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_step: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_step: basis not built");
     HvWeights w;
@@ -267,6 +272,7 @@ int ed_lanczos_step(const ed_sector* h, const double weights[4], int dtype, cons
 
 int ed_lanczos_hv(const ed_sector* h, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
                   void* v_next_dev, double* scal_dev, void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_lanczos_hv: empty sector");
     if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_hv: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_hv: basis not built");
     HvWeights w;
@@ -278,6 +284,7 @@ int ed_lanczos_hv(const ed_sector* h, const double weights[4], int dtype, const 
 
 int ed_lanczos_update(const ed_sector* h, int dtype, const void* v_dev, void* v_next_dev, const double* scal_dev,
                       void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_lanczos_update: empty sector");
     if (!h || !v_dev || !v_next_dev || !scal_dev) return set_error(ED_ERR_INVALID, "ed_lanczos_update: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_lanczos_update: basis not built");
     return lanczos_update_launch(h->s, dtype, v_dev, v_next_dev, scal_dev, (cudaStream_t)stream);
@@ -285,6 +292,7 @@ int ed_lanczos_update(const ed_sector* h, int dtype, const void* v_dev, void* v_
 
 int ed_accumulate(const ed_sector* h, int dtype, const void* x_dev, double coef_re, double coef_im, void* acc_dev,
                   void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return ED_OK;
     if (!h || !x_dev || !acc_dev) return set_error(ED_ERR_INVALID, "ed_accumulate: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_accumulate: basis not built");
     if (!std::isfinite(coef_re) || !std::isfinite(coef_im)) return set_error(ED_ERR_INVALID, "ed_accumulate: coef");
@@ -292,6 +300,7 @@ int ed_accumulate(const ed_sector* h, int dtype, const void* x_dev, double coef_
 }
 
 int ed_normalize(const ed_sector* h, int dtype, void* x_dev, double* norm_dev, void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_normalize: empty sector");
     if (!h || !x_dev || !norm_dev) return set_error(ED_ERR_INVALID, "ed_normalize: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_normalize: basis not built");
     return normalize_launch(h->s, dtype, x_dev, norm_dev, h->s.d_partials.p, (cudaStream_t)stream);

@@ -38,8 +38,10 @@ extern "C" {
 
 typedef struct ed_sector ed_sector;
 
-/* Sector of the periodic two-leg ladder: L rungs (1..16), Nh holes, Nd down
+/* Sector of the periodic two-leg ladder: L rungs (2..16), Nh holes, Nd down
  * spins, leg momentum kx (any integer, taken mod L) and rung parity ky (0/1).
+ * L = 1 is refused with ED_ERR_INVALID: its periodic leg bond would join a
+ * site to itself.  A sector without representatives is valid (n = 0).
  * Stands in for Hamiltonian_Config.get_translators()
  * (tJ_spin_half_ladder/matrix_setup.pyx:377-406), which builds
  * State_Index_Amplitude_Translator (symmetry_ladder.h:271-406) and
@@ -101,7 +103,9 @@ int ed_hv_mode(const ed_sector* s, const double weights[4], int dtype, const voi
  * be NULL (b_k ignored).  v_next receives v_{k+1}; it may alias v_prev.  The
  * products are accumulated in FP64 whatever dtype is.  When b_{k+1} < 1e-8
  * (the reference's breakdown test, :63-64) v_next is left as v' unnormalised
- * and scal_dev[3] is set to 1. */
+ * and scal_dev[3] is set to 1.  ed_lanczos_step, ed_lanczos_hv,
+ * ed_lanczos_update and ed_normalize refuse an empty sector (n = 0) with
+ * ED_ERR_INVALID; ed_hv, ed_hv_mode and ed_accumulate do nothing on one. */
 int ed_lanczos_step(const ed_sector* s, const double weights[4], int dtype, const void* v_dev, const void* v_prev_dev,
                     void* v_next_dev, double* scal_dev, void* stream);
 

@@ -191,7 +191,8 @@ __host__ __device__ __forceinline__ uint32_t compress_spins(uint32_t d, uint32_t
 // Colex rank of a compressed down mask from byte tables.  Chunk c covers compressed bits
 // 8c..8c+7; with k set bits below the chunk, T[off[c] + (k << sh[c]) + byte] is the sum over
 // the chunk's set bits (j-th from the bottom) of C(8c + bitpos, k + j).  The top chunk holds only
-// 2^(Ns - 8c) entries per k.
+// 2^(Ns - 8c) entries per k.  The mask must hold exactly Nd set bits (every configuration of the
+// sector does), so k stays within the table's Nd + 1 rows.
 struct RankTab {
     const uint32_t* T;
     uint32_t off[4];
@@ -199,6 +200,7 @@ struct RankTab {
 };
 
 __host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const RankTab& R, int Nd) {
+    (void)Nd;
     uint32_t r = 0;
     int k = 0;
 #pragma unroll
@@ -206,7 +208,6 @@ __host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const RankTa
         const uint32_t byte = (dc >> (8 * c)) & 255u;
         r += R.T[R.off[c] + ((uint32_t)k << R.sh[c]) + byte];
         k += popc32(byte);
-        if (k > Nd) k = Nd;
     }
     return r;
 }

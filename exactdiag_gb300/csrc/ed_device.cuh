@@ -375,6 +375,80 @@ __device__ __forceinline__ void gather_block(const typename Vec<R, CPLX>::T* __r
     }
 }
 
+// Exchange terms of a row of a free block: every neighbour is a representative of the same block
+// (orbit 2L, phase 1) at row ri +- delta, delta from the colex rank change of the swap.  Targets are
+// gathered kExBatch at a time (loads in flight per thread); bonds are taken from the highest bit
+// down, one find-leading-one each.  UNI (rung and leg exchange weights equal): the x_j are summed
+// with coefficient 1 and the sum scaled once; acc must be zero on entry.
+template <typename R, bool CPLX, bool UNI>
+__device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typename Vec<R, CPLX>::T* __restrict__ xb,
+                                              uint32_t ri, uint32_t dc, uint32_t mr, uint32_t ma, uint32_t m2,
+                                              uint32_t wrap_anti, const int (&wlo)[2], const int (&whi)[2], R cr,
+                                              R cl, int Nd, R& accr, R& acci) {
+    constexpr int kExBatch = 4;
+    uint32_t off[kExBatch];
+    R cb[kExBatch];
+    uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
+    while (m1) {
+        unsigned live = 0;
+#pragma unroll
+        for (int u = 0; u < kExBatch; ++u) {
+            off[u] = ri;
+            cb[u] = UNI ? R(1) : R(0);
+            if (m1) {
+                const int a = 31 - __clz(m1);
+                m1 ^= 1u << a;
+                const int k = __popc(dc & ((1u << a) - 1u));
+                const uint32_t delta = tb.comb[k * kCombStride + a];
+                off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
+                if constexpr (!UNI) cb[u] = ((mr >> a) & 1u) ? cr : cl;
+                live |= 1u << u;
+            }
+        }
+        gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
+    }
+    uint32_t mm = cl != R(0) ? m2 : 0u;
+    while (mm) {
+        unsigned live = 0;
+#pragma unroll
+        for (int u = 0; u < kExBatch; ++u) {
+            off[u] = ri;
+            cb[u] = UNI ? R(1) : R(0);
+            if (mm) {
+                const int a = 31 - __clz(mm);
+                mm ^= 1u << a;
+                const int k = __popc(dc & ((1u << a) - 1u));
+                const int mid = (dc >> (a + 1)) & 1u;
+                const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+                off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
+                if constexpr (!UNI) cb[u] = cl;
+                live |= 1u << u;
+            }
+        }
+        gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
+    }
+    if (cl != R(0) && wrap_anti) {
+        uint32_t offw[2];
+        R cw[2];
+        unsigned live = 0;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            offw[u] = ri;
+            cw[u] = UNI ? R(1) : R(0);
+            if ((wrap_anti >> u) & 1u) {
+                offw[u] = spin_rank(dc ^ (1u << wlo[u]) ^ (1u << whi[u]), tb.rank, Nd);
+                if constexpr (!UNI) cw[u] = cl;
+                live |= 1u << u;
+            }
+        }
+        gather_block<R, CPLX, 2>(xb, offw, live, cw, accr, acci);
+    }
+    if constexpr (UNI) {
+        accr *= cl;
+        if constexpr (CPLX) acci *= cl;
+    }
+}
+
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
@@ -417,64 +491,8 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         const R cr = R(0.5) * wr, cl = R(0.5) * wl;
         const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(x) + dstart;
         const uint32_t ri = (uint32_t)(i - dstart);
-        // exchange targets gathered kExBatch at a time (loads in flight per thread)
-        constexpr int kExBatch = 4;
-        uint32_t off[kExBatch];
-        R cb[kExBatch];
-        uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
-        while (m1) {
-            unsigned live = 0;
-#pragma unroll
-            for (int u = 0; u < kExBatch; ++u) {
-                off[u] = ri;
-                cb[u] = R(0);
-                if (m1) {
-                    const int a = __ffs(m1) - 1;
-                    m1 &= m1 - 1u;
-                    const int k = __popc(dc & ((1u << a) - 1u));
-                    const uint32_t delta = tb.comb[k * kCombStride + a];
-                    off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
-                    cb[u] = ((mr >> a) & 1u) ? cr : cl;
-                    live |= 1u << u;
-                }
-            }
-            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
-        }
-        uint32_t mm = cl != R(0) ? m2 : 0u;
-        while (mm) {
-            unsigned live = 0;
-#pragma unroll
-            for (int u = 0; u < kExBatch; ++u) {
-                off[u] = ri;
-                cb[u] = R(0);
-                if (mm) {
-                    const int a = __ffs(mm) - 1;
-                    mm &= mm - 1u;
-                    const int k = __popc(dc & ((1u << a) - 1u));
-                    const int mid = (dc >> (a + 1)) & 1u;
-                    const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
-                    off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
-                    cb[u] = cl;
-                    live |= 1u << u;
-                }
-            }
-            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
-        }
-        if (cl != R(0) && wrap_anti) {
-            unsigned live = 0;
-#pragma unroll
-            for (int u = 0; u < kExBatch; ++u) {
-                off[u] = ri;
-                cb[u] = R(0);
-                if (u < 2 && ((wrap_anti >> u) & 1u)) {
-                    const uint32_t dc2 = dc ^ (1u << wlo[u]) ^ (1u << whi[u]);
-                    off[u] = spin_rank(dc2, tb.rank, S.Nd);
-                    cb[u] = cl;
-                    live |= 1u << u;
-                }
-            }
-            gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
-        }
+        if (cr == cl) free_exchange<R, CPLX, true>(tb, xb, ri, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, S.Nd, accr, acci);
+        else free_exchange<R, CPLX, false>(tb, xb, ri, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, S.Nd, accr, acci);
     } else {
         // non-free block: each exchange target is resolved through the block's stabiliser (lowest
         // image, orbit, phase agreement), then its bitmap word

@@ -449,14 +449,142 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
     }
 }
 
+// A hop of the rows of a free block with everything that is the same for all of them folded in,
+// built once per chunk from the block's HopDesc and the weights (build_free_hops): the move of
+// the electron in compressed coordinates, the coset permutation of a free target, and the
+// coefficient.  For a free target the coefficient is w * sign * sqrt(2L) / sqrt(2L) times the
+// target's phase (exactly as the per-row path computes it); for a stabiliser target it is
+// w * sign * sqrt(2L), the orbit and phase of the target being resolved per row.
+template <typename R>
+struct alignas(16) FreeHop {
+    uint32_t keep;    // bits of the compressed mask that stay in place: ~(band | 1 << p)
+    uint32_t band;    // bits that shift by one position toward p
+    uint32_t shifts;  // sl | sr << 8 | p << 16 | q << 24: moved = ((dc & band) << sl) >> sr
+    uint32_t swap;    // target coset permutation (free targets): mirror pairs
+    uint32_t rot;     // rot | (Ns - rot) % 32 << 8 | mode << 16
+    uint32_t pad;
+    int64_t start;    // target block's first row (free targets)
+    R cr, ci;         // coefficient, real and imaginary parts
+};
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void build_free_hop(const HopDesc& H, const HvTables<R>& tb, const R w[4], int Ns, int N,
+                                               FreeHop<R>& F) {
+    const R wt = H.term ? w[1] : w[0];
+    const uint32_t mode = wt == R(0) ? (uint32_t)kModeAbsent : (uint32_t)H.mode;
+    const uint32_t sl = H.q > H.p ? 0u : 1u;
+    F.keep = ~(H.band | (1u << H.p));
+    F.band = H.band;
+    F.shifts = sl | ((1u - sl) << 8) | ((uint32_t)H.p << 16) | ((uint32_t)H.q << 24);
+    F.swap = H.swap;
+    F.rot = (uint32_t)H.rot | ((uint32_t)((Ns - H.rot) & 31) << 8) | (mode << 16);
+    F.pad = 0;
+    F.start = H.start;
+    const R base = ((uint8_t)H.sign == 1u ? -wt : wt) * tb.sqrtv[N];
+    if (mode == kModeFree) {
+        const R c = base * tb.rsqrtv[N];
+        if constexpr (CPLX) {
+            F.cr = c * tb.cosv[H.e];
+            F.ci = c * tb.sinv[H.e];
+        } else {
+            F.cr = H.e == 0 ? c : -c;
+            F.ci = R(0);
+        }
+    } else {
+        F.cr = base;
+        F.ci = R(0);
+    }
+}
+
+// The hops of a chunk's block (threads 0 .. nhop-1 build one each; the caller synchronises).
+template <typename R, bool CPLX>
+__device__ __forceinline__ void build_free_hops(const BlockDesc& D, const HvTables<R>& tb, const R w[4], int Ns, int N,
+                                                FreeHop<R>* shop) {
+    if (threadIdx.x < D.nhop) build_free_hop<R, CPLX>(D.hop[threadIdx.x], tb, w, Ns, N, shop[threadIdx.x]);
+}
+
+// Gathers of up to four targets with their coefficients already multiplied by the phase.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void gather4c(const void* __restrict__ x, const int64_t (&j)[4], const R (&cr)[4],
+                                         const R (&ci)[4], R& accr, R& acci) {
+    R xr[4], xi[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if (j[u] >= 0) ld<R, CPLX>(x, j[u], xr[u], xi[u]);
+        else xr[u] = xi[u] = R(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if constexpr (CPLX) {
+            accr += cr[u] * xr[u] - ci[u] * xi[u];
+            acci += cr[u] * xi[u] + ci[u] * xr[u];
+        } else {
+            accr += cr[u] * xr[u];
+        }
+    }
+}
+
+// Hops of a row of a free block (orbit 2L), four at a time, from the pre-built FreeHop records.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>& tb, const BlockDesc* __restrict__ D,
+                                          const FreeHop<R>* __restrict__ shop, int nhop, uint32_t dc, int Ns,
+                                          const void* __restrict__ x, R& accr, R& acci) {
+    const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
+#pragma unroll 1
+    for (int t0 = 0; t0 < nhop; t0 += 4) {
+        int64_t jj[4];
+        R cr[4], ci[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            jj[u] = -1;
+            cr[u] = ci[u] = R(0);
+            const int t = t0 + u;
+            if (t >= nhop) continue;
+            const FreeHop<R>& F = shop[t];
+            const uint4 f0 = reinterpret_cast<const uint4*>(&F)[0];  // keep, band, shifts, swap
+            const uint4 f1 = reinterpret_cast<const uint4*>(&F)[1];  // rot, pad, start
+            const uint32_t mode = (f1.x >> 16) & 255u;
+            if (mode == kModeAbsent) continue;
+            const uint32_t p = (f0.z >> 16) & 255u, q = f0.z >> 24;
+            const uint32_t moved = ((dc & f0.y) << (f0.z & 255u)) >> ((f0.z >> 8) & 255u);
+            const uint32_t dcm = (dc & f0.x) | moved | (((dc >> p) & 1u) << q);
+            if (mode == kModeFree) {
+                const uint32_t sw = swap_pairs(dcm, f0.w);
+                const uint32_t dct = ((sw << (f1.x & 255u)) | (sw >> ((f1.x >> 8) & 255u))) & nsmask;
+                jj[u] = (int64_t)(((uint64_t)f1.w << 32) | f1.z) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+                cr[u] = F.cr;
+                ci[u] = F.ci;
+            } else {
+                // stabiliser target: lowest coset image, its orbit and phase, then the bitmap
+                const HopDesc& H = D->hop[t];
+                const CandResult c2 = resolve_cand(H.cand, H.ncand, dcm, Ns);
+                if (!c2.valid) continue;
+                const int64_t j = bitmap_row(S, H.word_off, spin_rank(c2.best, tb.rank, S.Nd));
+                if (j < 0) continue;
+                const R c = F.cr * tb.rsqrtv[orbit_of_count(S.N, c2.count)];
+                jj[u] = j;
+                if constexpr (CPLX) {
+                    cr[u] = c * tb.cosv[c2.e];
+                    ci[u] = c * tb.sinv[c2.e];
+                } else {
+                    cr[u] = c2.e == 0 ? c : -c;
+                }
+            }
+        }
+        gather4c<R, CPLX>(x, jj, cr, ci, accr, acci);
+    }
+}
+
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
 // XIN: the caller has already loaded x_i into (xir, xii).
+// shop: the block's pre-built hops (ROWS == kRowsFree only).
 template <typename R, bool CPLX, int ROWS = 0, bool XIN = false>
 __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
                                             uint64_t key, const BlockDesc* __restrict__ D,
-                                            const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii) {
+                                            const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii,
+                                            const FreeHop<R>* __restrict__ shop = nullptr) {
     const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
     const int Ns = S.Ns, N = S.N;
     if constexpr (!XIN) ld<R, CPLX>(x, i, xir, xii);
@@ -521,6 +649,12 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
                 gather_add<R, CPLX>(x, j, coef * tb.rsqrtv[orbit_of_count(N, cr2.count)], cr2.e, tb, accr, acci);
             }
         }
+    }
+    if constexpr (ROWS == kRowsFree) {
+        free_hops<R, CPLX>(S, tb, D, shop, nhop, dc, Ns, x, accr, acci);
+        outr = accr + diag * xir;
+        outi = acci + diag * xii;
+        return;
     }
     // hops (tl, tr), four at a time
 #pragma unroll 1

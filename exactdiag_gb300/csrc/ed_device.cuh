@@ -449,14 +449,15 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
     }
 }
 
-// A hop of the rows of a free block with everything that is the same for all of them folded in,
-// built once per chunk from the block's HopDesc and the weights (build_free_hops): the move of
+// A hop of the rows of one block with everything that is the same for all of them folded in,
+// built once per chunk from the block's HopDesc and the weights (build_block_hops): the move of
 // the electron in compressed coordinates, the coset permutation of a free target, and the
-// coefficient.  For a free target the coefficient is w * sign * sqrt(2L) / sqrt(2L) times the
-// target's phase (exactly as the per-row path computes it); for a stabiliser target it is
-// w * sign * sqrt(2L), the orbit and phase of the target being resolved per row.
+// coefficient w * sign (times sqrt(2L) for rows of a free block, whose orbit is 2L; rows of a
+// stabiliser block multiply by sqrt of their own orbit).  For a free target the coefficient also
+// holds 1 / sqrt(2L) and the target's phase; for a stabiliser target the orbit and phase of the
+// target are resolved per row.
 template <typename R>
-struct alignas(16) FreeHop {
+struct alignas(16) BlockHop {
     uint32_t keep;    // bits of the compressed mask that stay in place: ~(band | 1 << p)
     uint32_t band;    // bits that shift by one position toward p
     uint32_t shifts;  // sl | sr << 8 | p << 16 | q << 24: moved = ((dc & band) << sl) >> sr
@@ -468,8 +469,8 @@ struct alignas(16) FreeHop {
 };
 
 template <typename R, bool CPLX>
-__device__ __forceinline__ void build_free_hop(const HopDesc& H, const HvTables<R>& tb, const R w[4], int Ns, int N,
-                                               FreeHop<R>& F) {
+__device__ __forceinline__ void build_block_hop(const HopDesc& H, const HvTables<R>& tb, const R w[4], int Ns, int N,
+                                                bool row_free, BlockHop<R>& F) {
     const R wt = H.term ? w[1] : w[0];
     const uint32_t mode = wt == R(0) ? (uint32_t)kModeAbsent : (uint32_t)H.mode;
     const uint32_t sl = H.q > H.p ? 0u : 1u;
@@ -480,7 +481,8 @@ __device__ __forceinline__ void build_free_hop(const HopDesc& H, const HvTables<
     F.rot = (uint32_t)H.rot | ((uint32_t)((Ns - H.rot) & 31) << 8) | (mode << 16);
     F.pad = 0;
     F.start = H.start;
-    const R base = ((uint8_t)H.sign == 1u ? -wt : wt) * tb.sqrtv[N];
+    const R sw = (uint8_t)H.sign == 1u ? -wt : wt;
+    const R base = row_free ? sw * tb.sqrtv[N] : sw;
     if (mode == kModeFree) {
         const R c = base * tb.rsqrtv[N];
         if constexpr (CPLX) {
@@ -498,9 +500,9 @@ __device__ __forceinline__ void build_free_hop(const HopDesc& H, const HvTables<
 
 // The hops of a chunk's block (threads 0 .. nhop-1 build one each; the caller synchronises).
 template <typename R, bool CPLX>
-__device__ __forceinline__ void build_free_hops(const BlockDesc& D, const HvTables<R>& tb, const R w[4], int Ns, int N,
-                                                FreeHop<R>* shop) {
-    if (threadIdx.x < D.nhop) build_free_hop<R, CPLX>(D.hop[threadIdx.x], tb, w, Ns, N, shop[threadIdx.x]);
+__device__ __forceinline__ void build_block_hops(const BlockDesc& D, const HvTables<R>& tb, const R w[4], int Ns, int N,
+                                                 bool row_free, BlockHop<R>* shop) {
+    if (threadIdx.x < D.nhop) build_block_hop<R, CPLX>(D.hop[threadIdx.x], tb, w, Ns, N, row_free, shop[threadIdx.x]);
 }
 
 // Gathers of up to four targets with their coefficients already multiplied by the phase.
@@ -524,11 +526,12 @@ __device__ __forceinline__ void gather4c(const void* __restrict__ x, const int64
     }
 }
 
-// Hops of a row of a free block (orbit 2L), four at a time, from the pre-built FreeHop records.
-template <typename R, bool CPLX>
-__device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>& tb, const BlockDesc* __restrict__ D,
-                                          const FreeHop<R>* __restrict__ shop, int nhop, uint32_t dc, int Ns,
-                                          const void* __restrict__ x, R& accr, R& acci) {
+// Hops of a row, four at a time, from the pre-built BlockHop records.  ROW_FREE: the row's orbit
+// (2L) is folded into the records; otherwise every coefficient is scaled by sqNi = sqrt(orbit).
+template <typename R, bool CPLX, bool ROW_FREE>
+__device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R>& tb, const BlockDesc* __restrict__ D,
+                                           const BlockHop<R>* __restrict__ shop, int nhop, uint32_t dc, int Ns, R sqNi,
+                                           const void* __restrict__ x, R& accr, R& acci) {
     const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
 #pragma unroll 1
     for (int t0 = 0; t0 < nhop; t0 += 4) {
@@ -540,7 +543,7 @@ __device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>
             cr[u] = ci[u] = R(0);
             const int t = t0 + u;
             if (t >= nhop) continue;
-            const FreeHop<R>& F = shop[t];
+            const BlockHop<R>& F = shop[t];
             const uint4 f0 = reinterpret_cast<const uint4*>(&F)[0];  // keep, band, shifts, swap
             const uint4 f1 = reinterpret_cast<const uint4*>(&F)[1];  // rot, pad, start
             const uint32_t mode = (f1.x >> 16) & 255u;
@@ -552,8 +555,8 @@ __device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>
                 const uint32_t sw = swap_pairs(dcm, f0.w);
                 const uint32_t dct = ((sw << (f1.x & 255u)) | (sw >> ((f1.x >> 8) & 255u))) & nsmask;
                 jj[u] = (int64_t)(((uint64_t)f1.w << 32) | f1.z) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
-                cr[u] = F.cr;
-                ci[u] = F.ci;
+                cr[u] = ROW_FREE ? F.cr : F.cr * sqNi;
+                ci[u] = ROW_FREE ? F.ci : F.ci * sqNi;
             } else {
                 // stabiliser target: lowest coset image, its orbit and phase, then the bitmap
                 const HopDesc& H = D->hop[t];
@@ -561,7 +564,8 @@ __device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>
                 if (!c2.valid) continue;
                 const int64_t j = bitmap_row(S, H.word_off, spin_rank(c2.best, tb.rank, S.Nd));
                 if (j < 0) continue;
-                const R c = F.cr * tb.rsqrtv[orbit_of_count(S.N, c2.count)];
+                R c = F.cr * tb.rsqrtv[orbit_of_count(S.N, c2.count)];
+                if constexpr (!ROW_FREE) c *= sqNi;
                 jj[u] = j;
                 if constexpr (CPLX) {
                     cr[u] = c * tb.cosv[c2.e];
@@ -575,16 +579,85 @@ __device__ __forceinline__ void free_hops(const SectorView& S, const HvTables<R>
     }
 }
 
+// A stabiliser of two elements {identity, g} (cand[0], cand[1] of a block with ncand == 2), with
+// the images under g of every bond flip built once per chunk (build_pair_stab): an exchange
+// target's image is then g(dc) ^ g(flip).
+struct PairStab {
+    uint32_t gf1[32];  // g(1 << a | 1 << (a + 1))
+    uint32_t gf2[32];  // g(1 << a | 1 << (a + 2))
+    uint32_t gfw[2];   // g of the flips of the wrap bonds
+    int e0, eg;        // phase exponents of the identity and of g
+};
+
+// Threads 0..31 fill one position each (the caller synchronises).  Only for ncand == 2.
+__device__ __forceinline__ void build_pair_stab(const BlockDesc& D, int Ns, PairStab& P) {
+    const int a = threadIdx.x;
+    if (a < 32) {
+        const CandParams& g = D.cand[1];
+        P.gf1[a] = a + 1 < Ns ? cand_image(g, (1u << a) | (2u << a), Ns) : 0u;
+        P.gf2[a] = a + 2 < Ns ? cand_image(g, (1u << a) | (4u << a), Ns) : 0u;
+        if (a < 2) P.gfw[a] = a < D.nwrap ? cand_image(g, (1u << D.wrap[a][0]) | (1u << D.wrap[a][1]), Ns) : 0u;
+        if (a == 0) {
+            P.e0 = D.cand[0].e;
+            P.eg = g.e;
+        }
+    }
+}
+
+// Exchange terms of a row of a block whose stabiliser is {identity, g}: the target t = dc ^ flip
+// and its image g(t) = g(dc) ^ g(flip) (the flip's image from P); the lower of the two is the
+// representative, t == g(t) halves the orbit and needs the phases of identity and g to agree
+// (the reference's amplitude test, symmetry_ladder.h:196-224), then the bitmap gives its row.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void pair_exchange(const SectorView& S, const HvTables<R>& tb, const PairStab& P,
+                                              const CandParams& g, int64_t word_off, uint32_t dc, uint32_t mr,
+                                              uint32_t ma, uint32_t m2, uint32_t wrap_anti, const int (&wlo)[2],
+                                              const int (&whi)[2], R cr, R cl, int Ns, int N,
+                                              const void* __restrict__ x, R& accr, R& acci) {
+    const uint32_t gx = cand_image(g, dc, Ns);
+    const R rN = tb.rsqrtv[N], rN2 = tb.rsqrtv[N >> 1];
+    const int e0 = P.e0, eg = P.eg;
+    const bool phases_agree = e0 == eg;
+#pragma unroll 1
+    for (int kind = 0; kind < 4; ++kind) {
+        uint32_t m;
+        int dist;
+        R coef;
+        const uint32_t* gtab;
+        if (kind == 0) { m = mr; dist = 1; coef = cr; gtab = P.gf1; }
+        else if (kind == 1) { m = ma; dist = 1; coef = cl; gtab = P.gf1; }
+        else if (kind == 2) { m = m2; dist = 2; coef = cl; gtab = P.gf2; }
+        else { m = wrap_anti; dist = 0; coef = cl; gtab = P.gfw; }
+        if (coef == R(0)) continue;
+        const R c1 = coef * rN, c2 = coef * rN2;
+        while (m) {
+            const int a = 31 - __clz(m);
+            m ^= 1u << a;
+            const uint32_t flip = dist ? ((1u << a) | (1u << (a + dist)))
+                                       : ((1u << (a ? wlo[1] : wlo[0])) | (1u << (a ? whi[1] : whi[0])));
+            const uint32_t t = dc ^ flip, gt = gx ^ gtab[a];
+            const bool eq = gt == t;
+            if (eq && !phases_agree) continue;
+            const bool lower = gt < t;
+            const int64_t j = bitmap_row(S, word_off, spin_rank(lower ? gt : t, tb.rank, S.Nd));
+            if (j < 0) continue;
+            gather_add<R, CPLX>(x, j, eq ? c2 : c1, lower ? eg : e0, tb, accr, acci);
+        }
+    }
+}
+
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
 // XIN: the caller has already loaded x_i into (xir, xii).
-// shop: the block's pre-built hops (ROWS == kRowsFree only).
+// shop: the block's pre-built hops, pstab: its two-element stabiliser when ncand == 2 (both used
+// only by the kind-specialised rows, ROWS != 0).
 template <typename R, bool CPLX, int ROWS = 0, bool XIN = false>
 __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
                                             uint64_t key, const BlockDesc* __restrict__ D,
                                             const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii,
-                                            const FreeHop<R>* __restrict__ shop = nullptr) {
+                                            const BlockHop<R>* __restrict__ shop = nullptr,
+                                            const PairStab* __restrict__ pstab = nullptr) {
     const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
     const int Ns = S.Ns, N = S.N;
     if constexpr (!XIN) ld<R, CPLX>(x, i, xir, xii);
@@ -627,8 +700,12 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         const int ncand = (dw1.x >> 16) & 255u;
         const int64_t word_off = D->word_off;
         const R cr = R(0.5) * wr * sqNi, cl = R(0.5) * wl * sqNi;
+        if (ROWS != 0 && ncand == 2) {
+            pair_exchange<R, CPLX>(S, tb, *pstab, D->cand[1], word_off, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, Ns,
+                                   N, x, accr, acci);
+        }
 #pragma unroll 1
-        for (int kind = 0; kind < 4; ++kind) {
+        for (int kind = 0; kind < (ROWS != 0 && ncand == 2 ? 0 : 4); ++kind) {
             uint32_t m;
             int dist;
             R coef;
@@ -650,8 +727,8 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
             }
         }
     }
-    if constexpr (ROWS == kRowsFree) {
-        free_hops<R, CPLX>(S, tb, D, shop, nhop, dc, Ns, x, accr, acci);
+    if constexpr (ROWS != 0) {
+        block_hops<R, CPLX, ROWS == kRowsFree>(S, tb, D, shop, nhop, dc, Ns, sqNi, x, accr, acci);
         outr = accr + diag * xir;
         outi = acci + diag * xii;
         return;

@@ -89,14 +89,16 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
     const HvTables<R> tb = load_tables<R>(views[0], smem);
     const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
     __shared__ __align__(16) BlockDesc sdesc;
-    __shared__ FreeHop<R> shop[KIND == kRowsFree ? kMaxHops : 1];
+    __shared__ BlockHop<R> shop[KIND == kRowsGeneric ? 1 : kMaxHops];
+    __shared__ PairStab pstab;
     for (int c = blockIdx.x; c < count; c += gridDim.x) {
         const int cid = idx[c];
         const BatchChunk ch = chunks[cid];
         const SectorView S = views[ch.sec];
         if constexpr (KIND != kRowsGeneric) stage_block(S.desc + ch.block, &sdesc);
-        if constexpr (KIND == kRowsFree) {
-            build_free_hops<R, CPLX>(sdesc, tb, w, S.Ns, S.N, shop);
+        if constexpr (KIND != kRowsGeneric) {
+            build_block_hops<R, CPLX>(sdesc, tb, w, S.Ns, S.N, KIND == kRowsFree, shop);
+            if (KIND == kRowsCand && sdesc.ncand == 2) build_pair_stab(sdesc, S.Ns, pstab);
             __syncthreads();
         }
         const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
                     if (!first) ld<R, CPLX>(yp, in, pr_n, pi_n);
                 }
                 R hr, hi;
-                hv_row_fast<R, CPLX, KIND, true>(S, tb, w, i, key, &sdesc, x, hr, hi, xr, xi, shop);
+                hv_row_fast<R, CPLX, KIND, true>(S, tb, w, i, key, &sdesc, x, hr, hi, xr, xi, shop, &pstab);
                 finish_row(i, hr, hi, xr, xi, pr, pi);
                 key = key_n;
                 xr = xr_n;

@@ -376,56 +376,52 @@ __device__ __forceinline__ void gather_block(const typename Vec<R, CPLX>::T* __r
 }
 
 // Exchange terms of a row of a free block: every neighbour is a representative of the same block
-// (orbit 2L, phase 1) at row ri +- delta, delta from the colex rank change of the swap.  Targets are
-// gathered kExBatch at a time (loads in flight per thread); bonds are taken from the highest bit
-// down, one find-leading-one each.  UNI (rung and leg exchange weights equal): the x_j are summed
-// with coefficient 1 and the sum scaled once; acc must be zero on entry.
+// (orbit 2L, phase 1) at row ri +- delta, delta from the colex rank change of the swap.  Bonds
+// are taken from the highest bit down, one find-leading-one each, in counted loops unrolled by
+// four (independent gathers in flight per thread).  UNI (rung and leg exchange weights equal):
+// the x_j are summed with coefficient 1 and the sum scaled once; acc must be zero on entry.
 template <typename R, bool CPLX, bool UNI>
 __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typename Vec<R, CPLX>::T* __restrict__ xb,
                                               uint32_t ri, uint32_t dc, uint32_t mr, uint32_t ma, uint32_t m2,
                                               uint32_t wrap_anti, const int (&wlo)[2], const int (&whi)[2], R cr,
                                               R cl, int Nd, R& accr, R& acci) {
-    constexpr int kExBatch = 4;
-    uint32_t off[kExBatch];
-    R cb[kExBatch];
     uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
-    while (m1) {
-        unsigned live = 0;
-#pragma unroll
-        for (int u = 0; u < kExBatch; ++u) {
-            off[u] = ri;
-            cb[u] = UNI ? R(1) : R(0);
-            if (m1) {
-                const int a = 31 - __clz(m1);
-                m1 ^= 1u << a;
-                const int k = __popc(dc & ((1u << a) - 1u));
-                const uint32_t delta = tb.comb[k * kCombStride + a];
-                off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
-                if constexpr (!UNI) cb[u] = ((mr >> a) & 1u) ? cr : cl;
-                live |= 1u << u;
-            }
+    const int n1 = __popc(m1);
+#pragma unroll 4
+    for (int q = 0; q < n1; ++q) {
+        const int a = 31 - __clz(m1);
+        const uint32_t bit = 1u << a;
+        m1 ^= bit;
+        const int k = __popc(dc & (bit - 1u));
+        const uint32_t delta = tb.comb[k * kCombStride + a];
+        const uint32_t o = (dc & bit) ? ri + delta : ri - delta;
+        R xr, xi;
+        ld<R, CPLX>(xb, o, xr, xi);
+        if constexpr (UNI) {
+            accr += xr;
+            if constexpr (CPLX) acci += xi;
+        } else {
+            const R c = (mr & bit) ? cr : cl;
+            accr += c * xr;
+            if constexpr (CPLX) acci += c * xi;
         }
-        gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
     }
     uint32_t mm = cl != R(0) ? m2 : 0u;
-    while (mm) {
-        unsigned live = 0;
-#pragma unroll
-        for (int u = 0; u < kExBatch; ++u) {
-            off[u] = ri;
-            cb[u] = UNI ? R(1) : R(0);
-            if (mm) {
-                const int a = 31 - __clz(mm);
-                mm ^= 1u << a;
-                const int k = __popc(dc & ((1u << a) - 1u));
-                const int mid = (dc >> (a + 1)) & 1u;
-                const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
-                off[u] = ((dc >> a) & 1u) ? ri + delta : ri - delta;
-                if constexpr (!UNI) cb[u] = cl;
-                live |= 1u << u;
-            }
-        }
-        gather_block<R, CPLX, kExBatch>(xb, off, live, cb, accr, acci);
+    const int n2 = __popc(mm);
+#pragma unroll 4
+    for (int q = 0; q < n2; ++q) {
+        const int a = 31 - __clz(mm);
+        const uint32_t bit = 1u << a;
+        mm ^= bit;
+        const int k = __popc(dc & (bit - 1u));
+        const int mid = (dc >> (a + 1)) & 1u;
+        const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+        const uint32_t o = (dc & bit) ? ri + delta : ri - delta;
+        R xr, xi;
+        ld<R, CPLX>(xb, o, xr, xi);
+        const R c = UNI ? R(1) : cl;
+        accr += c * xr;
+        if constexpr (CPLX) acci += c * xi;
     }
     if (cl != R(0) && wrap_anti) {
         uint32_t offw[2];
@@ -456,17 +452,21 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
 // stabiliser block multiply by sqrt of their own orbit).  For a free target the coefficient also
 // holds 1 / sqrt(2L) and the target's phase; for a stabiliser target the orbit and phase of the
 // target are resolved per row.
+// Every field is a full word, read as four 16-byte words without unpacking.
 template <typename R>
 struct alignas(16) BlockHop {
     uint32_t keep;    // bits of the compressed mask that stay in place: ~(band | 1 << p)
     uint32_t band;    // bits that shift by one position toward p
-    uint32_t shifts;  // sl | sr << 8 | p << 16 | q << 24: moved = ((dc & band) << sl) >> sr
+    uint32_t sl, sr;  // moved = ((dc & band) << sl) >> sr
+    uint32_t p, q;    // the electron's compressed position before and after
     uint32_t swap;    // target coset permutation (free targets): mirror pairs
-    uint32_t rot;     // rot | (Ns - rot) % 32 << 8 | mode << 16
-    uint32_t pad;
+    uint32_t rot;     // and left rotation by rot ...
+    uint32_t nsr;     // ... as (x << rot | x >> nsr) & mask, nsr = (Ns - rot) % 32
+    uint32_t mode;    // kModeFree / kModeCand / kModeAbsent (weight zero)
     int64_t start;    // target block's first row (free targets)
     R cr, ci;         // coefficient, real and imaginary parts
 };
+static_assert(sizeof(BlockHop<float>) == 64 && sizeof(BlockHop<double>) == 64, "BlockHop is four 16-byte words");
 
 template <typename R, bool CPLX>
 __device__ __forceinline__ void build_block_hop(const HopDesc& H, const HvTables<R>& tb, const R w[4], int Ns, int N,
@@ -476,10 +476,14 @@ __device__ __forceinline__ void build_block_hop(const HopDesc& H, const HvTables
     const uint32_t sl = H.q > H.p ? 0u : 1u;
     F.keep = ~(H.band | (1u << H.p));
     F.band = H.band;
-    F.shifts = sl | ((1u - sl) << 8) | ((uint32_t)H.p << 16) | ((uint32_t)H.q << 24);
+    F.sl = sl;
+    F.sr = 1u - sl;
+    F.p = H.p;
+    F.q = H.q;
     F.swap = H.swap;
-    F.rot = (uint32_t)H.rot | ((uint32_t)((Ns - H.rot) & 31) << 8) | (mode << 16);
-    F.pad = 0;
+    F.rot = H.rot;
+    F.nsr = (uint32_t)((Ns - H.rot) & 31);
+    F.mode = mode;
     F.start = H.start;
     const R sw = (uint8_t)H.sign == 1u ? -wt : wt;
     const R base = row_free ? sw * tb.sqrtv[N] : sw;
@@ -544,17 +548,16 @@ __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R
             const int t = t0 + u;
             if (t >= nhop) continue;
             const BlockHop<R>& F = shop[t];
-            const uint4 f0 = reinterpret_cast<const uint4*>(&F)[0];  // keep, band, shifts, swap
-            const uint4 f1 = reinterpret_cast<const uint4*>(&F)[1];  // rot, pad, start
-            const uint32_t mode = (f1.x >> 16) & 255u;
-            if (mode == kModeAbsent) continue;
-            const uint32_t p = (f0.z >> 16) & 255u, q = f0.z >> 24;
-            const uint32_t moved = ((dc & f0.y) << (f0.z & 255u)) >> ((f0.z >> 8) & 255u);
-            const uint32_t dcm = (dc & f0.x) | moved | (((dc >> p) & 1u) << q);
-            if (mode == kModeFree) {
-                const uint32_t sw = swap_pairs(dcm, f0.w);
-                const uint32_t dct = ((sw << (f1.x & 255u)) | (sw >> ((f1.x >> 8) & 255u))) & nsmask;
-                jj[u] = (int64_t)(((uint64_t)f1.w << 32) | f1.z) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+            const uint4 f0 = reinterpret_cast<const uint4*>(&F)[0];  // keep, band, sl, sr
+            const uint4 f1 = reinterpret_cast<const uint4*>(&F)[1];  // p, q, swap, rot
+            const uint4 f2 = reinterpret_cast<const uint4*>(&F)[2];  // nsr, mode, start
+            if (f2.y == kModeAbsent) continue;
+            const uint32_t moved = ((dc & f0.y) << f0.z) >> f0.w;
+            const uint32_t dcm = (dc & f0.x) | moved | (((dc >> f1.x) & 1u) << f1.y);
+            if (f2.y == kModeFree) {
+                const uint32_t sw = swap_pairs(dcm, f1.z);
+                const uint32_t dct = ((sw << f1.w) | (sw >> f2.x)) & nsmask;
+                jj[u] = (int64_t)(((uint64_t)f2.w << 32) | f2.z) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
                 cr[u] = ROW_FREE ? F.cr : F.cr * sqNi;
                 ci[u] = ROW_FREE ? F.ci : F.ci * sqNi;
             } else {

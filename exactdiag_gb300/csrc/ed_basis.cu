@@ -297,12 +297,7 @@ __global__ void export_sparse_kernel(SectorView S, uint64_t n_spin, int64_t* __r
     for (int i = threadIdx.x; i < kCombStride * kCombStride; i += blockDim.x) s_comb[i] = S.comb[i];
     for (int i = threadIdx.x; i < tab_words; i += blockDim.x) s_rank[i] = S.rank_tab[i];
     __syncthreads();
-    RankTab rt;
-    rt.T = s_rank;
-    for (int c = 0; c < 4; ++c) {
-        rt.off[c] = S.rk_off[c];
-        rt.sh[c] = S.rk_sh[c];
-    }
+    const RankTab rt = rank_tab_of(S, s_rank);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < S.n; i += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t key = S.keys[i];
         const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;

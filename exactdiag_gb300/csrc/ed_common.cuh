@@ -125,9 +125,11 @@ struct SectorView {
     const uint64_t* bitmap;        // candidate bitmaps of every block (basis construction only)
     const int64_t* word_prefix;    // dense row of the first set bit of each bitmap word (construction only)
     const ulonglong2* bitpref;     // {bitmap word, its prefix} side by side: one 16-byte load per lookup
-    const uint32_t* rank_tab;      // byte tables of the colex spin rank (compact layout, see RankTab)
-    uint32_t rk_off[4];            // first word of byte-chunk c's table
-    uint32_t rk_sh[4];             // log2 of the entries per k of chunk c (8, or fewer for the top chunk)
+    const uint32_t* rank_tab;      // tables of the colex spin rank (layout: see RankTab)
+    uint32_t rk_off[4];            // first word of chunk c's table
+    uint32_t rk_pos[4];            // first compressed bit of chunk c (c >= 1)
+    uint32_t rk_m0;                // bits of chunk 0
+    uint32_t rk_nch;               // number of chunks, 3 or 4
     int rank_words;                // words of rank_tab
     const uint32_t* comb;          // [33][33] comb[k*33+n] = C(n,k)
     const BlockDesc* desc;         // [n_blocks] fast-row descriptors (null: the orbit-walk row only)
@@ -188,28 +190,46 @@ __host__ __device__ __forceinline__ uint32_t compress_spins(uint32_t d, uint32_t
     return d;
 }
 
-// Colex rank of a compressed down mask from byte tables.  Chunk c covers compressed bits
-// 8c..8c+7; with k set bits below the chunk, T[off[c] + (k << sh[c]) + byte] is the sum over
-// the chunk's set bits (j-th from the bottom) of C(8c + bitpos, k + j).  The top chunk holds only
-// 2^(Ns - 8c) entries per k.  The mask must hold exactly Nd set bits (every configuration of the
-// sector does), so k stays within the table's Nd + 1 rows.
+// Colex rank of a compressed down mask from tables, three lookups for Ns <= 28.  Chunk 0 covers
+// compressed bits [0, w0) (m0 = 2^w0 - 1), which have no set bits below them: T[dc & m0] is the
+// sum over its set bits (j-th from the bottom, at position b) of C(b, j).  Chunks c = 1 .. nch-1
+// cover the eight bits from pos[c]; with k set bits below the chunk, T[off[c] + (k << 8) + byte]
+// is the sum over the byte's set bits of C(pos[c] + b, k + j).  nch = 3 and w0 = max(0, Ns - 16)
+// for Ns <= 28, else nch = 4 and w0 = Ns - 24.  The mask must hold exactly Nd set bits (every
+// configuration of the sector does), so k stays within the Nd + 1 rows of each chunk.
 struct RankTab {
     const uint32_t* T;
+    uint32_t m0;
+    uint32_t nch;
     uint32_t off[4];
-    uint32_t sh[4];
+    uint32_t pos[4];
 };
 
 __host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const RankTab& R, int Nd) {
     (void)Nd;
-    uint32_t r = 0;
-    int k = 0;
+    uint32_t r = R.T[dc & R.m0];
+    uint32_t k = (uint32_t)popc32(dc & R.m0);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        const uint32_t byte = (dc >> (8 * c)) & 255u;
-        r += R.T[R.off[c] + ((uint32_t)k << R.sh[c]) + byte];
-        k += popc32(byte);
+    for (int c = 1; c < 4; ++c) {
+        if (c == 3 && R.nch < 4) break;
+        const uint32_t byte = (dc >> R.pos[c]) & 255u;
+        r += R.T[R.off[c] + (k << 8) + byte];
+        k += (uint32_t)popc32(byte);
     }
     return r;
+}
+
+// RankTab over a copy T of the sector's rank tables.
+__host__ __device__ __forceinline__ RankTab rank_tab_of(const SectorView& S, const uint32_t* T) {
+    RankTab rt;
+    rt.T = T;
+    rt.m0 = S.rk_m0;
+    rt.nch = S.rk_nch;
+    for (int c = 0; c < 4; ++c) {
+        rt.off[c] = S.rk_off[c];
+        rt.pos[c] = S.rk_pos[c];
+    }
+    return rt;
 }
 
 // Colex rank of a hole mask (general/symmetry_ladder.h:346-361, hole part).

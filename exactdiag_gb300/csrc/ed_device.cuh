@@ -841,14 +841,7 @@ __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
         s_rsqrt[i] = i ? (R)(1.0 / sqrt((double)i)) : R(0);
     }
     __syncthreads();
-    RankTab rt;
-    rt.T = s_rank;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        rt.off[c] = S.rk_off[c];
-        rt.sh[c] = S.rk_sh[c];
-    }
-    return HvTables<R>{rt, s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
+    return HvTables<R>{rank_tab_of(S, s_rank), s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
 }
 
 inline size_t hv_smem_bytes(const SectorView& S, size_t real_size) {

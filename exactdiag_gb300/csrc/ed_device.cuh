@@ -50,6 +50,7 @@ template <typename R>
 struct HvTables {
     RankTab rank;          // shared
     const uint32_t* comb;  // shared
+    const uint32_t* d2;    // shared: [(k * 32 + a) * 2 + mid] = C(a, k) + C(a + 1, k + mid), k <= Nd
     const R* cosv;         // cos(pi e / L), e in [0, 2L)
     const R* sinv;         // +sin(pi e / L): conj(u^e) = cos + i sin
     const R* sqrtv;        // sqrt(k), k in [0, 32]
@@ -415,7 +416,7 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
         mm ^= bit;
         const int k = __popc(dc & (bit - 1u));
         const int mid = (dc >> (a + 1)) & 1u;
-        const uint32_t delta = tb.comb[k * kCombStride + a] + tb.comb[(k + mid) * kCombStride + a + 1];
+        const uint32_t delta = tb.d2[(k * 32 + a) * 2 + mid];
         const uint32_t o = (dc & bit) ? ri + delta : ri - delta;
         R xr, xi;
         ld<R, CPLX>(xb, o, xr, xi);
@@ -823,13 +824,19 @@ __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
     uint32_t* s_rank = reinterpret_cast<uint32_t*>(smem);
     const int tab_words = S.rank_words;
     uint32_t* s_comb = s_rank + ((tab_words + 1) & ~1);
-    R* s_f = reinterpret_cast<R*>(s_comb + kCombStride * kCombStride + 1);  // 8-byte aligned (odd count + 1)
+    uint32_t* s_d2 = s_comb + kCombStride * kCombStride + 1;  // 8-byte aligned (odd count + 1)
+    const int d2_words = (S.Nd + 1) * 64;
+    R* s_f = reinterpret_cast<R*>(s_d2 + d2_words);
     R* s_cos = s_f;
     R* s_sin = s_f + 64;
     R* s_sqrt = s_f + 128;
     R* s_rsqrt = s_f + 161;
     for (int i = threadIdx.x; i < tab_words; i += blockDim.x) s_rank[i] = S.rank_tab[i];
     for (int i = threadIdx.x; i < kCombStride * kCombStride; i += blockDim.x) s_comb[i] = S.comb[i];
+    for (int i = threadIdx.x; i < d2_words; i += blockDim.x) {
+        const int k = i >> 6, a = (i >> 1) & 31, mid = i & 1;
+        s_d2[i] = S.comb[k * kCombStride + a] + (k + mid <= kMaxN ? S.comb[(k + mid) * kCombStride + a + 1] : 0u);
+    }
     for (int i = threadIdx.x; i < 2 * S.L; i += blockDim.x) {
         double c, s;
         sincospi((double)i / (double)S.L, &s, &c);
@@ -841,11 +848,11 @@ __device__ HvTables<R> load_tables(const SectorView& S, uint8_t* smem) {
         s_rsqrt[i] = i ? (R)(1.0 / sqrt((double)i)) : R(0);
     }
     __syncthreads();
-    return HvTables<R>{rank_tab_of(S, s_rank), s_comb, s_cos, s_sin, s_sqrt, s_rsqrt};
+    return HvTables<R>{rank_tab_of(S, s_rank), s_comb, s_d2, s_cos, s_sin, s_sqrt, s_rsqrt};
 }
 
 inline size_t hv_smem_bytes(const SectorView& S, size_t real_size) {
-    return (((S.rank_words + 1) & ~1) + kCombStride * kCombStride + 1) * sizeof(uint32_t) +
+    return (((S.rank_words + 1) & ~1) + kCombStride * kCombStride + 1 + (S.Nd + 1) * 64) * sizeof(uint32_t) +
            (64 + 64 + 33 + 33) * real_size;
 }
 

@@ -368,7 +368,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
 
 // The fused H.v pass of one step over every row kind of a plan (device tables in `a`, whose idx
 // points at the whole kind-ordered id list), one launch per kind present.
-static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, const int kind_first[4],
+static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, int cand_grid_f32, const int kind_first[4],
                        const int kind_count[4], StepArgs a, cudaStream_t st) {
     const int* idx0 = a.idx;
     a.idx = idx0 + kind_first[kRowsFree];
@@ -377,8 +377,9 @@ static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, const
     if (int rc = step_hv_free(dtype, minb, a, st)) return rc;
     a.idx = idx0 + kind_first[kRowsCand];
     a.count = kind_count[kRowsCand];
-    a.grid = other_grid;
+    a.grid = dtype == ED_F32 ? cand_grid_f32 : other_grid;
     if (int rc = step_hv_cand(dtype, a, st)) return rc;
+    a.grid = other_grid;
     a.idx = idx0 + kind_first[kRowsGeneric];
     a.count = kind_count[kRowsGeneric];
     return step_hv_generic(dtype, a, st);
@@ -452,7 +453,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         void* other = b[(k + 1) % 2];
         StepArgs a{dviews.p, doffs.p, dchunks.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
                     partials.p};
-        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid,
+        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid, s0.cand_grid_f32,
                                  plan.kind_first, plan.kind_count, a, cap)) {
             if (use_graph) {
                 cudaGraph_t g = nullptr;
@@ -555,7 +556,7 @@ static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, c
                            double* scal, cudaStream_t st) {
     StepArgs a{s.d_self.p, s.d_offs.p, s.d_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
                const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p};
-    if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.hv_grid, s.other_grid, s.kind_first,
+    if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.hv_grid, s.other_grid, s.cand_grid_f32, s.kind_first,
                              s.kind_count, a, st))
         return rc;
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
@@ -573,7 +574,8 @@ int set_launch(Sector& s, int minb, int ctas_per_sm) {
     const int per_sm = (ctas_per_sm == 0 || ctas_per_sm > occ) ? occ : ctas_per_sm;
     s.hv_minb = minb;
     s.hv_grid = s.num_sms * per_sm;
-    s.other_grid = s.num_sms * step_rest_occupancy(smem);
+    s.other_grid = s.num_sms * step_rest_occupancy(smem, false);
+    s.cand_grid_f32 = s.num_sms * step_rest_occupancy(smem, true);
     return ED_OK;
 }
 

@@ -66,7 +66,7 @@ constexpr int kHvThreads = 256;
 constexpr int kReduceSlots = 4;  // FP64 partial sums per chunk in the fused Lanczos step
 // Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
 // (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
-constexpr int kChunkRows = 4096;
+constexpr int kChunkRows = 8192;
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
 enum RowKind : int {
@@ -110,6 +110,7 @@ struct Sector {
     int hv_grid = 0;             // persistent grid of the H.v kernels (free-row step kernel)
     int hv_minb = 3;             // launch variant of the free-row step kernel (minimum resident CTAs per SM)
     int other_grid = 0;          // grid of the other row kinds' step kernels
+    int cand_grid_f32 = 0;       // grid of the stabiliser-row kernel for real FP32 vectors
     std::vector<BlockSpan> spans;  // host copy of the blocks' row ranges and kinds
     DevBuf<uint32_t> d_comb;     // [33][33]
     DevBuf<uint32_t> d_rank_tab; // [4][Nd+1][256]
@@ -183,7 +184,7 @@ int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st);
 int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st);
 int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st);
 int step_free_occupancy(int minb, size_t smem);
-int step_rest_occupancy(size_t smem);
+int step_rest_occupancy(size_t smem, bool f32);
 int singlet_corr_launch(const Sector& s, int dtype, const void* psi, const int* fixed, double* out, cudaStream_t st);
 int corr_launch(const Sector& s, int dtype, const void* psi, int kind, int nfixed, const int* fixed, double* out,
                 cudaStream_t st);

@@ -4,12 +4,17 @@
 
 namespace ed {
 
-int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st) { return step_kind_dtype<3, kRowsCand>(dtype, a, st); }
+// Real FP32 rows fit a 4-CTA register budget without spilling; the wider types keep 3.
+int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st) {
+    return dtype == ED_F32 ? launch_step_kind<float, false, 4, kRowsCand>(a, st) : step_kind_dtype<3, kRowsCand>(dtype, a, st);
+}
 
 int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st) {
     return step_kind_dtype<3, kRowsGeneric>(dtype, a, st);
 }
 
-int step_rest_occupancy(size_t smem) { return step_kind_occupancy<3, kRowsCand>(smem); }
+int step_rest_occupancy(size_t smem, bool f32) {
+    return f32 ? step_kind_occupancy<4, kRowsCand>(smem) : step_kind_occupancy<3, kRowsCand>(smem);
+}
 
 }  // namespace ed

@@ -40,7 +40,7 @@ METRIC = "Lanczos steps/s & HÂ·v HBM GB/s, 2Ã—14 t-J: mixed vs FP64 GPU at Î”Eâ‰
 UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
-KERNEL_VERSION = "v6"  # the H.v kernel generation the committed traffic figure was captured on
+KERNEL_VERSION = "v7"  # the H.v kernel generation the committed traffic figure was captured on
 
 
 def workload_name(sector) -> str:
@@ -114,8 +114,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def ncu_traffic(workload_key: str) -> float | None:
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if it covers this workload."""
+def ncu_traffic(workload_key: str, kind_rows: tuple[int, int, int]) -> float | None:
+    """DRAM bytes of one fused H.v step (all row kinds) from the committed ncu summary: its bytes
+    per row of each kind times this sector's rows of that kind, if the summary covers this workload
+    and kernel generation."""
     p = ROOT / "profiles" / "lanczos_hv_2x14_traffic.txt"
     if not p.exists():
         return None
@@ -126,7 +128,9 @@ def ncu_traffic(workload_key: str) -> float | None:
             fields[k.strip()] = v.strip()
     if fields.get("workload") != workload_key or fields.get("kernel_version") != KERNEL_VERSION:
         return None
-    return float(fields["dram_bytes_per_launch"])
+    per_row = [float(fields["dram_bytes_per_row_free"]), float(fields["dram_bytes_per_row_stabiliser"]),
+               float(fields.get("dram_bytes_per_row_orbit_walk", fields["dram_bytes_per_row_stabiliser"]))]
+    return sum(r * b for r, b in zip(kind_rows, per_row))
 
 
 def aggregate_replicas(ms_local: list[float], steps: int, world: int, device=None) -> tuple[list[float], float]:
@@ -242,7 +246,7 @@ def run_engine(args, rank: int, world: int) -> dict | None:
 
     if rank != 0:
         return None
-    traffic = ncu_traffic(workload_name(SECTOR))
+    traffic = ncu_traffic(workload_name(SECTOR), autotune.kind_rows(sec))
     return {
         "metric": METRIC,
         "value": value,

@@ -76,6 +76,13 @@ def row_kinds(sector: DeviceSector) -> tuple[int, int, int]:
     return int(c[0]), int(c[1]), int(c[2])
 
 
+def kind_rows(sector: DeviceSector) -> tuple[int, int, int]:
+    """Rows per row kind (free, stabiliser-resolved, orbit walk)."""
+    c = (ctypes.c_int64 * 3)()
+    nat.check("ed_sector_kind_rows", sector._lib.ed_sector_kind_rows(sector.handle, c))
+    return int(c[0]), int(c[1]), int(c[2])
+
+
 def step_launches(sector: DeviceSector) -> int:
     """Kernel launches of one ed_lanczos_step: one fused H.v kernel per row kind present, the
     scalar reduction, and the update (flat pass, exact-norm pass, exact b, scaling pass)."""

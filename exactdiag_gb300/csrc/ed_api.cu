@@ -210,6 +210,18 @@ int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
     return ED_OK;
 }
 
+int ed_sector_kind_rows(const ed_sector* h, int64_t rows[3]) {
+    if (!h || !rows) return set_error(ED_ERR_INVALID, "ed_sector_kind_rows: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_kind_rows: basis not built");
+    rows[0] = rows[1] = rows[2] = 0;
+    for (const BlockSpan& b : h->s.spans) {
+        if (b.kind == kRowsFree) rows[0] += b.count;
+        else if (b.kind == kRowsCand) rows[1] += b.count;
+        else rows[2] += b.count;
+    }
+    return ED_OK;
+}
+
 int ed_basis_size(const ed_sector* h, int64_t* n) {
     if (!h || !n) return set_error(ED_ERR_INVALID, "ed_basis_size: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_basis_size: basis not built");

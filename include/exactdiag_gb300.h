@@ -60,11 +60,14 @@ int ed_basis_build(ed_sector* s, void* stream);
 int ed_sector_set_launch(ed_sector* s, int min_ctas_per_sm, int ctas_per_sm);
 int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
 
-/* Chunks of the sector's fused step per row kind: counts[0] rows of blocks with a trivial
- * stabiliser (colex-delta rows), counts[1] rows of blocks with a small stabiliser (coset
- * candidates + bitmap), counts[2] rows taking the orbit walk.  Each non-zero count is one
+/* Chunks of the sector's fused step per row kind: counts[0] chunks of rows of blocks with a
+ * trivial stabiliser (colex-delta rows), counts[1] chunks of rows of blocks with a small
+ * stabiliser (coset candidates + bitmap), counts[2] chunks of rows taking the orbit walk.  Each non-zero count is one
  * kernel launch per step.  No reference counterpart (a property of this engine's layout). */
 int ed_sector_row_kinds(const ed_sector* sector, int counts[3]);
+
+/* Rows of the sector per row kind, in the order of ed_sector_row_kinds. */
+int ed_sector_kind_rows(const ed_sector* sector, int64_t rows[3]);
 
 /* Number of representatives (Basis_Index_Map::get_num_states, basis_indexing.h:180-182). */
 int ed_basis_size(const ed_sector* s, int64_t* n);

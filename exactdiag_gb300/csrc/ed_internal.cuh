@@ -64,8 +64,9 @@ inline int grid_for(int64_t work, int threads, int sms, int per_sm = 8) {
 
 constexpr int kHvThreads = 256;
 constexpr int kReduceSlots = 4;  // FP64 partial sums per chunk in the fused Lanczos step
-// Rows per chunk: small enough that the CTAs running at one time cover a narrow window of rows
-// (the gathered x_j of neighbouring rows stay in L2), large enough to amortise the per-chunk reduction.
+// Rows per chunk (at most; plan_chunks halves it for row kinds with few rows): small enough that the
+// CTAs running at one time cover a narrow window of rows (the gathered x_j of neighbouring rows
+// stay in L2), large enough to amortise the per-chunk reduction and descriptor staging.
 constexpr int kChunkRows = 8192;
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
@@ -113,7 +114,7 @@ struct Sector {
     int cand_grid_f32 = 0;       // grid of the stabiliser-row kernel for real FP32 vectors
     std::vector<BlockSpan> spans;  // host copy of the blocks' row ranges and kinds
     DevBuf<uint32_t> d_comb;     // [33][33]
-    DevBuf<uint32_t> d_rank_tab; // [4][Nd+1][256]
+    DevBuf<uint32_t> d_rank_tab; // colex spin-rank tables (layout: RankTab)
     DevBuf<BlockInfo> d_blocks;
     DevBuf<HoleEntry> d_holes;
     DevBuf<uint64_t> d_bitmap;

@@ -333,29 +333,29 @@ __global__ void __launch_bounds__(kUpdThreads, 4)
 
 // Chunks of every sector: each block's rows cut every chunk_rows[kind] (a chunk never straddles
 // two blocks), sector-major in row order; the chunk ids grouped by row kind.  A kind's chunks are
-// kChunkRows long, halved (down to kChunkRows / 8) while the kind would have fewer chunks than
-// four per SM, so that small kinds still spread over the whole GPU.
+// kChunkRows long, halved (down to kChunkRows / 8) while the sector's rows of that kind would
+// make fewer chunks than four per SM, so that small kinds still spread over the whole GPU.  The
+// lengths depend on the sector alone: a sector is cut the same way alone and in a batch, so its
+// per-chunk sums, and with them its recursion, are the same bits either way.
 void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
     const int nsec = (int)secs.size();
     P.chunks.clear();
     P.kind_idx.clear();
     P.cfirst.assign(nsec, 0);
     P.ccount.assign(nsec, 0);
-    int64_t kind_rows[4] = {0, 0, 0, 0};
-    for (const Sector* S : secs) {
-        if (S->spans.empty()) kind_rows[kRowsGeneric] += S->view.n;
-        for (const BlockSpan& sp : S->spans) kind_rows[sp.kind] += sp.count;
-    }
-    const int64_t want = 4 * (int64_t)(nsec > 0 && secs[0]->num_sms > 0 ? secs[0]->num_sms : 1);
-    int64_t chunk_rows[4];
-    for (int kind = 0; kind < 4; ++kind) {
-        chunk_rows[kind] = kChunkRows;
-        while (chunk_rows[kind] > kChunkRows / 8 && kind_rows[kind] / chunk_rows[kind] < want) chunk_rows[kind] /= 2;
-    }
     std::vector<int> by_kind[4];
     for (int s = 0; s < nsec; ++s) {
         const Sector& S = *secs[s];
         P.cfirst[s] = (int)P.chunks.size();
+        int64_t kind_rows[4] = {0, 0, 0, 0};
+        if (S.spans.empty()) kind_rows[kRowsGeneric] += S.view.n;
+        for (const BlockSpan& sp : S.spans) kind_rows[sp.kind] += sp.count;
+        const int64_t want = 4 * (int64_t)(S.num_sms > 0 ? S.num_sms : 1);
+        int64_t chunk_rows[4];
+        for (int kind = 0; kind < 4; ++kind) {
+            chunk_rows[kind] = kChunkRows;
+            while (chunk_rows[kind] > kChunkRows / 8 && kind_rows[kind] / chunk_rows[kind] < want) chunk_rows[kind] /= 2;
+        }
         auto add_span = [&](int64_t start, int64_t count, int block, int kind) {
             const int64_t cr = chunk_rows[kind];
             for (int64_t b = 0; b < count; b += cr) {

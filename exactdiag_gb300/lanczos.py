@@ -38,11 +38,11 @@ class LanczosRun:
 
         autotune.ensure(sector, self.weights, dtype)
 
-    def _record(self, ritz=None, acc=None) -> None:
+    def _record(self, ritz=None, acc=None, steps: int | None = None) -> None:
         s = self.sector
         s.normalize(self.buf[0], self.norm)
         self.scal.zero_()
-        for k in range(self.m):
+        for k in range(self.m if steps is None else min(steps, self.m)):
             v = self.buf[k % 2]
             other = self.buf[(k + 1) % 2]
             if ritz is not None and k < len(ritz):
@@ -56,8 +56,9 @@ class LanczosRun:
             self._record()
             return
         if self.graph is None:
-            # warm up outside capture (sets kernel attributes), then capture
-            self._record()
+            # warm up outside capture with two steps (every kernel of the recursion launches once
+            # and sets its attributes), then capture the whole recursion
+            self._record(steps=2)
             self.buf[0].copy_(v0)
             torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()

@@ -469,11 +469,20 @@ struct alignas(16) BlockHop {
 };
 static_assert(sizeof(BlockHop<float>) == 64 && sizeof(BlockHop<double>) == 64, "BlockHop is four 16-byte words");
 
+// BlockHop mode of a free target reached without a coset permutation (rot = 0, no mirror pairs)
+// by a move of at most one compressed position, from a row of a free block: the target's spin
+// rank is the row's own rank (its offset in the block) plus the rank change of one adjacent swap.
+constexpr uint32_t kHopDelta = 4;
+
 template <typename R, bool CPLX>
 __device__ __forceinline__ void build_block_hop(const HopDesc& H, const HvTables<R>& tb, const R w[4], int Ns, int N,
                                                 bool row_free, BlockHop<R>& F) {
     const R wt = H.term ? w[1] : w[0];
-    const uint32_t mode = wt == R(0) ? (uint32_t)kModeAbsent : (uint32_t)H.mode;
+    uint32_t mode = wt == R(0) ? (uint32_t)kModeAbsent : (uint32_t)H.mode;
+    const int dpq = (int)H.p - (int)H.q;
+    if (row_free && mode == kModeFree && H.rot == 0 && H.swap == 0 && dpq >= -1 && dpq <= 1 &&
+        H.band == (dpq == 0 ? 0u : (1u << H.q)))
+        mode = kHopDelta;
     const uint32_t sl = H.q > H.p ? 0u : 1u;
     F.keep = ~(H.band | (1u << H.p));
     F.band = H.band;
@@ -488,7 +497,7 @@ __device__ __forceinline__ void build_block_hop(const HopDesc& H, const HvTables
     F.start = H.start;
     const R sw = (uint8_t)H.sign == 1u ? -wt : wt;
     const R base = row_free ? sw * tb.sqrtv[N] : sw;
-    if (mode == kModeFree) {
+    if (mode == kModeFree || mode == kHopDelta) {
         const R c = base * tb.rsqrtv[N];
         if constexpr (CPLX) {
             F.cr = c * tb.cosv[H.e];
@@ -533,10 +542,11 @@ __device__ __forceinline__ void gather4c(const void* __restrict__ x, const int64
 
 // Hops of a row, four at a time, from the pre-built BlockHop records.  ROW_FREE: the row's orbit
 // (2L) is folded into the records; otherwise every coefficient is scaled by sqNi = sqrt(orbit).
+// ri: the row's offset in its block (= its spin rank), used by kHopDelta records (free rows only).
 template <typename R, bool CPLX, bool ROW_FREE>
 __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R>& tb, const BlockDesc* __restrict__ D,
-                                           const BlockHop<R>* __restrict__ shop, int nhop, uint32_t dc, int Ns, R sqNi,
-                                           const void* __restrict__ x, R& accr, R& acci) {
+                                           const BlockHop<R>* __restrict__ shop, int nhop, uint32_t dc, uint32_t ri,
+                                           int Ns, R sqNi, const void* __restrict__ x, R& accr, R& acci) {
     const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
 #pragma unroll 1
     for (int t0 = 0; t0 < nhop; t0 += 4) {
@@ -553,6 +563,20 @@ __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R
             const uint4 f1 = reinterpret_cast<const uint4*>(&F)[1];  // p, q, swap, rot
             const uint4 f2 = reinterpret_cast<const uint4*>(&F)[2];  // nsr, mode, start
             if (f2.y == kModeAbsent) continue;
+            if (ROW_FREE && f2.y == kHopDelta) {
+                // adjacent swap of compressed positions p, q (or none when p == q)
+                const uint32_t lo = min(f1.x, f1.y);
+                const uint32_t bit = 1u << lo;
+                uint32_t r = ri;
+                if (((dc >> f1.x) ^ (dc >> f1.y)) & 1u) {
+                    const uint32_t delta = tb.comb[__popc(dc & (bit - 1u)) * kCombStride + lo];
+                    r = (dc & bit) ? ri + delta : ri - delta;
+                }
+                jj[u] = (int64_t)(((uint64_t)f2.w << 32) | f2.z) + (int64_t)r;
+                cr[u] = F.cr;
+                ci[u] = F.ci;
+                continue;
+            }
             const uint32_t moved = ((dc & f0.y) << f0.z) >> f0.w;
             const uint32_t dcm = (dc & f0.x) | moved | (((dc >> f1.x) & 1u) << f1.y);
             if (f2.y == kModeFree) {
@@ -732,7 +756,8 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         }
     }
     if constexpr (ROWS != 0) {
-        block_hops<R, CPLX, ROWS == kRowsFree>(S, tb, D, shop, nhop, dc, Ns, sqNi, x, accr, acci);
+        block_hops<R, CPLX, ROWS == kRowsFree>(S, tb, D, shop, nhop, dc, (uint32_t)(i - dstart), Ns, sqNi, x, accr,
+                                               acci);
         outr = accr + diag * xir;
         outi = acci + diag * xii;
         return;

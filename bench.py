@@ -58,7 +58,8 @@ def peaks() -> tuple[float, str]:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running; mark() before and
+    after the timed region selects the samples taken during it (plus the first one after)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -74,7 +75,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -95,10 +96,24 @@ class ClockSampler:
             if self.thread is not None:
                 self.thread.join(timeout=2)
 
-    def summary(self) -> dict:
+    def wait_first(self, timeout_s: float = 3.0) -> None:
+        """Block until the sampler has produced a sample (nvidia-smi takes a moment to start)."""
+        t_end = time.perf_counter() + timeout_s
+        while self.proc is not None and not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.02)
+
+    def mark(self) -> int:
+        return len(self.lines)
+
+    def wait_one_more(self, n: int, timeout_s: float = 0.5) -> None:
+        t_end = time.perf_counter() + timeout_s
+        while self.proc is not None and len(self.lines) <= n and time.perf_counter() < t_end:
+            time.sleep(0.01)
+
+    def summary(self, lo: int = 0, hi: int | None = None) -> dict:
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[lo: None if hi is None else hi + 1]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -193,25 +208,29 @@ def run_engine(args, rank: int, world: int) -> dict | None:
                 ev[1].record()
             sec.lanczos_update(v, other, scal[2 * k: 2 * k + 4])
 
-        for k in range(W):
-            step(k)
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
         with ClockSampler(dev.index) as clocks:
+            clocks.wait_first()
+            for k in range(W):
+                step(k)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            lo = clocks.mark()
             start.record()
             for k in range(W, W + K):
                 step(k, evs[k - W])
             stop.record()
             torch.cuda.synchronize()
+            hi = clocks.mark()
+            clocks.wait_one_more(hi)
         if world > 1:
             torch.distributed.barrier()
         total_ms = start.elapsed_time(stop)
         hv_ms = [a.elapsed_time(b) for a, b in evs]
-        return total_ms, hv_ms, clocks.summary(), dt
+        return total_ms, hv_ms, clocks.summary(lo, hi), dt
 
     total_mixed, hv_mixed, clocks, dt_mixed = timed_steps("fp32")
     total_fp64, hv_fp64, _, dt64 = timed_steps("fp64")

@@ -13,22 +13,26 @@ from conftest import seeded_vector
 pytestmark = pytest.mark.gpu
 
 W = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
+# weight sets that take the step kernels' other branches: rung and leg exchange weights that differ
+# (per-bond coefficients), terms switched off (absent hops, one exchange kind off), negative hopping
+WEIGHTS = [W, {"tl": 1.0, "tr": 0.7, "jl": 0.5, "jr": 0.3}, {"tl": 1.0, "tr": 0.0, "jl": 0.5, "jr": 0.5},
+           {"tl": 0.0, "tr": -1.3, "jl": 0.0, "jr": 0.4}, {"tl": 0.6, "tr": 1.0, "jl": 0.35, "jr": 0.0}]
 SMALL = [(6, 2, 5, kx, ky) for kx in range(6) for ky in (0, 1)] + [(7, 3, 5, 2, 1), (8, 4, 6, 3, 0), (6, 0, 6, 1, 1),
                                                                    (8, 1, 7, 5, 1), (5, 5, 0, 0, 0)]
 FULL = [(12, 2, 11, kx, ky) for kx in range(12) for ky in (0, 1)]
 
 
-def _check(torch, key, precision, tol):
+def _check(torch, key, precision, tol, w=W):
     from exactdiag_gb300.engine import DeviceSector
 
     sec = DeviceSector(*key)
     dt = sec.dtype(precision)
     x = seeded_vector(sec.n, 17, not sec.is_real)
     v = torch.as_tensor(x if not sec.is_real else x.real, device=sec.device).to(dt)
-    ref = sec.hv(v, W)
+    ref = sec.hv(v, w)
     y = torch.zeros_like(v)
     scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
-    sec.lanczos_hv(W, v, None, y, scal[0:4])
+    sec.lanczos_hv(w, v, None, y, scal[0:4])
     torch.cuda.synchronize()
     scale = max(1.0, float(torch.max(torch.abs(ref)).item()))
     err = float(torch.max(torch.abs(y - ref)).item())
@@ -41,8 +45,31 @@ def _check(torch, key, precision, tol):
 
 @pytest.mark.parametrize("key", SMALL)
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_step_kernel_equals_hv_small(cuda, key, precision):
-    _check(cuda, key, precision, 1e-12 if precision == "fp64" else 1e-6)
+@pytest.mark.parametrize("w", range(len(WEIGHTS)))
+def test_step_kernel_equals_hv_small(cuda, key, precision, w):
+    _check(cuda, key, precision, 1e-12 if precision == "fp64" else 1e-6, WEIGHTS[w])
+
+
+@pytest.mark.parametrize("key", [(6, 2, 5, 1, 1), (7, 3, 5, 2, 1), (5, 2, 4, 0, 0)])
+@pytest.mark.parametrize("w", range(1, len(WEIGHTS)))
+def test_step_kernel_vs_oracle_weights(cuda, oracle, key, w):
+    """The step kernel's y = H v against the oracle's matrix directly, for the weight sets that
+    take the per-bond coefficient, absent-hop and exchange-off branches."""
+    torch = cuda
+    from exactdiag_gb300.engine import DeviceSector
+
+    weights = WEIGHTS[w]
+    sec = DeviceSector(*key)
+    osec = oracle.Sector(*key)
+    h = oracle.hamiltonian(osec, weights, oracle.basis(osec))
+    x = seeded_vector(sec.n, 29, not sec.is_real)
+    if sec.is_real:
+        x = x.real
+    v = torch.as_tensor(x, device=sec.device)
+    y = torch.zeros_like(v)
+    scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
+    sec.lanczos_hv(weights, v, None, y, scal[0:4])
+    assert np.max(np.abs(y.cpu().numpy() - h @ x)) < 1e-12
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

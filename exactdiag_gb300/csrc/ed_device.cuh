@@ -386,9 +386,11 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
                                               uint32_t ri, uint32_t dc, uint32_t mr, uint32_t ma, uint32_t m2,
                                               uint32_t wrap_anti, const int (&wlo)[2], const int (&whi)[2], R cr,
                                               R cl, int Nd, R& accr, R& acci) {
+    // unroll factor: four FP32 gathers in flight; two for FP64 (measured: fewer registers win there)
+    constexpr int kUnroll = sizeof(R) == 4 ? 4 : 2;
     uint32_t m1 = (cr != R(0) ? mr : 0u) | (cl != R(0) ? ma : 0u);
     const int n1 = __popc(m1);
-#pragma unroll 4
+#pragma unroll kUnroll
     for (int q = 0; q < n1; ++q) {
         const int a = 31 - __clz(m1);
         const uint32_t bit = 1u << a;
@@ -409,7 +411,7 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
     }
     uint32_t mm = cl != R(0) ? m2 : 0u;
     const int n2 = __popc(mm);
-#pragma unroll 4
+#pragma unroll kUnroll
     for (int q = 0; q < n2; ++q) {
         const int a = 31 - __clz(mm);
         const uint32_t bit = 1u << a;
@@ -758,56 +760,54 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
     if constexpr (ROWS != 0) {
         block_hops<R, CPLX, ROWS == kRowsFree>(S, tb, D, shop, nhop, dc, (uint32_t)(i - dstart), Ns, sqNi, x, accr,
                                                acci);
-        outr = accr + diag * xir;
-        outi = acci + diag * xii;
-        return;
-    }
-    // hops (tl, tr), four at a time
+    } else {
+        // hops (tl, tr), four at a time
 #pragma unroll 1
-    for (int t0 = 0; t0 < nhop; t0 += 4) {
+        for (int t0 = 0; t0 < nhop; t0 += 4) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            jj[u] = -1;
-            cc[u] = R(0);
-            ee[u] = 0;
-            const int t = t0 + u;
-            if (t >= nhop) continue;
-            const HopDesc& H = D->hop[t];
-            // hot words: {band, swap, p|q|rot|e, term|mode|ncand|sign}, {start, word_off}
-            const uint4 hw = reinterpret_cast<const uint4*>(&H)[0];
-            const uint32_t hmode = (hw.w >> 8) & 255u;
-            const R wt = (hw.w & 255u) ? w[1] : w[0];
-            if (wt == R(0) || hmode == kModeAbsent) continue;
-            const R coef = ((hw.w >> 24) == 1u ? -wt : wt) * sqNi;
-            // (blocks with such hops are orbit-walk blocks: the kind-specialised kernels never see one)
-            if (ROWS == 0 && hmode == kModeGeneric) {
-                const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
-                const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
-                add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
-                continue;
+            for (int u = 0; u < 4; ++u) {
+                jj[u] = -1;
+                cc[u] = R(0);
+                ee[u] = 0;
+                const int t = t0 + u;
+                if (t >= nhop) continue;
+                const HopDesc& H = D->hop[t];
+                // hot words: {band, swap, p|q|rot|e, term|mode|ncand|sign}, {start, word_off}
+                const uint4 hw = reinterpret_cast<const uint4*>(&H)[0];
+                const uint32_t hmode = (hw.w >> 8) & 255u;
+                const R wt = (hw.w & 255u) ? w[1] : w[0];
+                if (wt == R(0) || hmode == kModeAbsent) continue;
+                const R coef = ((hw.w >> 24) == 1u ? -wt : wt) * sqNi;
+                // (blocks with such hops are orbit-walk blocks: the kind-specialised kernels never see one)
+                if (ROWS == 0 && hmode == kModeGeneric) {
+                    const uint32_t h2 = h ^ (1u << H.a) ^ (1u << H.b);
+                    const uint32_t d2 = ((d >> H.a) & 1u) ? (d ^ (1u << H.a) ^ (1u << H.b)) : d;
+                    add_target<R, CPLX>(S, tb, h2, d2, coef, x, accr, acci);
+                    continue;
+                }
+                const uint4 hw1 = reinterpret_cast<const uint4*>(&H)[1];
+                const int p = hw.z & 255u, q = (hw.z >> 8) & 255u;
+                const uint32_t band = hw.x;
+                const uint32_t moved = (q > p) ? ((dc & band) >> 1) : ((dc & band) << 1);
+                const uint32_t dcm = (dc & ~(band | (1u << p))) | moved | (((dc >> p) & 1u) << q);
+                if (hmode == kModeFree) {
+                    const uint32_t dct = rot_ns(swap_pairs(dcm, hw.y), (hw.z >> 16) & 255u, Ns);
+                    jj[u] = (int64_t)(((uint64_t)hw1.y << 32) | hw1.x) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
+                    cc[u] = coef * tb.rsqrtv[N];
+                    ee[u] = hw.z >> 24;
+                } else {
+                    const CandResult cr2 = resolve_cand(H.cand, (hw.w >> 16) & 255u, dcm, Ns);
+                    if (!cr2.valid) continue;
+                    const int64_t j =
+                        bitmap_row(S, (int64_t)(((uint64_t)hw1.w << 32) | hw1.z), spin_rank(cr2.best, tb.rank, S.Nd));
+                    if (j < 0) continue;
+                    jj[u] = j;
+                    cc[u] = coef * tb.rsqrtv[orbit_of_count(N, cr2.count)];
+                    ee[u] = cr2.e;
+                }
             }
-            const uint4 hw1 = reinterpret_cast<const uint4*>(&H)[1];
-            const int p = hw.z & 255u, q = (hw.z >> 8) & 255u;
-            const uint32_t band = hw.x;
-            const uint32_t moved = (q > p) ? ((dc & band) >> 1) : ((dc & band) << 1);
-            const uint32_t dcm = (dc & ~(band | (1u << p))) | moved | (((dc >> p) & 1u) << q);
-            if (hmode == kModeFree) {
-                const uint32_t dct = rot_ns(swap_pairs(dcm, hw.y), (hw.z >> 16) & 255u, Ns);
-                jj[u] = (int64_t)(((uint64_t)hw1.y << 32) | hw1.x) + (int64_t)spin_rank(dct, tb.rank, S.Nd);
-                cc[u] = coef * tb.rsqrtv[N];
-                ee[u] = hw.z >> 24;
-            } else {
-                const CandResult cr2 = resolve_cand(H.cand, (hw.w >> 16) & 255u, dcm, Ns);
-                if (!cr2.valid) continue;
-                const int64_t j =
-                    bitmap_row(S, (int64_t)(((uint64_t)hw1.w << 32) | hw1.z), spin_rank(cr2.best, tb.rank, S.Nd));
-                if (j < 0) continue;
-                jj[u] = j;
-                cc[u] = coef * tb.rsqrtv[orbit_of_count(N, cr2.count)];
-                ee[u] = cr2.e;
-            }
+            gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
         }
-        gather4<R, CPLX>(x, jj, cc, ee, tb, accr, acci);
     }
     outr = accr + diag * xir;
     outi = acci + diag * xii;

@@ -521,18 +521,18 @@ __device__ __forceinline__ void build_block_hops(const BlockDesc& D, const HvTab
     if (threadIdx.x < D.nhop) build_block_hop<R, CPLX>(D.hop[threadIdx.x], tb, w, Ns, N, row_free, shop[threadIdx.x]);
 }
 
-// Gathers of up to four targets with their coefficients already multiplied by the phase.
-template <typename R, bool CPLX>
-__device__ __forceinline__ void gather4c(const void* __restrict__ x, const int64_t (&j)[4], const R (&cr)[4],
-                                         const R (&ci)[4], R& accr, R& acci) {
-    R xr[4], xi[4];
+// Gathers of up to K targets with their coefficients already multiplied by the phase.
+template <typename R, bool CPLX, int K>
+__device__ __forceinline__ void gather_kc(const void* __restrict__ x, const int64_t (&j)[K], const R (&cr)[K],
+                                          const R (&ci)[K], R& accr, R& acci) {
+    R xr[K], xi[K];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < K; ++u) {
         if (j[u] >= 0) ld<R, CPLX>(x, j[u], xr[u], xi[u]);
         else xr[u] = xi[u] = R(0);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < K; ++u) {
         if constexpr (CPLX) {
             accr += cr[u] * xr[u] - ci[u] * xi[u];
             acci += cr[u] * xi[u] + ci[u] * xr[u];
@@ -542,20 +542,22 @@ __device__ __forceinline__ void gather4c(const void* __restrict__ x, const int64
     }
 }
 
-// Hops of a row, four at a time, from the pre-built BlockHop records.  ROW_FREE: the row's orbit
-// (2L) is folded into the records; otherwise every coefficient is scaled by sqNi = sqrt(orbit).
+// Hops of a row, four (FP32) or two (FP64) at a time, from the pre-built BlockHop records.
+// ROW_FREE: the row's orbit (2L) is folded into the records; otherwise every coefficient is scaled
+// by sqNi = sqrt(orbit).
 // ri: the row's offset in its block (= its spin rank), used by kHopDelta records (free rows only).
 template <typename R, bool CPLX, bool ROW_FREE>
 __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R>& tb, const BlockDesc* __restrict__ D,
                                            const BlockHop<R>* __restrict__ shop, int nhop, uint32_t dc, uint32_t ri,
                                            int Ns, R sqNi, const void* __restrict__ x, R& accr, R& acci) {
     const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
+    constexpr int kB = sizeof(R) == 4 ? 4 : 2;  // targets in flight: four FP32, two FP64
 #pragma unroll 1
-    for (int t0 = 0; t0 < nhop; t0 += 4) {
-        int64_t jj[4];
-        R cr[4], ci[4];
+    for (int t0 = 0; t0 < nhop; t0 += kB) {
+        int64_t jj[kB];
+        R cr[kB], ci[kB];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kB; ++u) {
             jj[u] = -1;
             cr[u] = ci[u] = R(0);
             const int t = t0 + u;
@@ -605,7 +607,7 @@ __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R
                 }
             }
         }
-        gather4c<R, CPLX>(x, jj, cr, ci, accr, acci);
+        gather_kc<R, CPLX, kB>(x, jj, cr, ci, accr, acci);
     }
 }
 

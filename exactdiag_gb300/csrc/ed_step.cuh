@@ -5,9 +5,10 @@
 //   y_i = (H v)_i - b_k v_{k-1,i}                    (general/cython_lanczos_diagonalization.pyx:68-77)
 // stores y_i, and accumulates the chunk's partial sums <v,Hv>, |y|^2, <v,y>, |v|^2 (per thread
 // exactly, see Accum; per chunk in FP64).  Every row of a chunk lies in one block, so the CTA
-// stages that block's descriptor once per chunk.  Instantiations by row kind keep each kernel's
-// register budget to the code its rows need: free blocks never touch the coset or bitmap code of
-// the others.
+// stages that block's descriptor once per chunk and builds from it what all its rows share: the
+// hop records (BlockHop) and, for a two-element stabiliser, the images of the bond flips
+// (PairStab).  Instantiations by row kind keep each kernel's register budget to the code its rows
+// need: free blocks never touch the coset or bitmap code of the others.
 #pragma once
 
 #include "ed_device.cuh"
@@ -95,8 +96,9 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
         const int cid = idx[c];
         const BatchChunk ch = chunks[cid];
         const SectorView S = views[ch.sec];
-        if constexpr (KIND != kRowsGeneric) stage_block(S.desc + ch.block, &sdesc);
         if constexpr (KIND != kRowsGeneric) {
+            // stage_block's first barrier also ends the previous chunk's reads of shop and pstab
+            stage_block(S.desc + ch.block, &sdesc);
             build_block_hops<R, CPLX>(sdesc, tb, w, S.Ns, S.N, KIND == kRowsFree, shop);
             if (KIND == kRowsCand && sdesc.ncand == 2) build_pair_stab(sdesc, S.Ns, pstab);
             __syncthreads();

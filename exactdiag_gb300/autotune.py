@@ -85,8 +85,10 @@ def kind_rows(sector: DeviceSector) -> tuple[int, int, int]:
 
 def step_launches(sector: DeviceSector) -> int:
     """Kernel launches of one ed_lanczos_step: one fused H.v kernel per row kind present, the
-    scalar reduction, and the update (flat pass, exact-norm pass, exact b, scaling pass)."""
-    return sum(1 for c in row_kinds(sector) if c > 0) + 1 + 4
+    expansion of the stabiliser blocks when there are any, the scalar reduction, and the update
+    (flat pass, exact-norm pass, exact b, scaling pass)."""
+    kinds = row_kinds(sector)
+    return sum(1 for c in kinds if c > 0) + (1 if kinds[1] > 0 else 0) + 1 + 4
 
 
 _MEMO: dict = {}

@@ -343,6 +343,8 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
     P.kind_idx.clear();
     P.cfirst.assign(nsec, 0);
     P.ccount.assign(nsec, 0);
+    P.tasks.clear();
+    P.n_full = 0;
     std::vector<int> by_kind[4];
     for (int s = 0; s < nsec; ++s) {
         const Sector& S = *secs[s];
@@ -358,12 +360,19 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
         }
         auto add_span = [&](int64_t start, int64_t count, int block, int kind) {
             const int64_t cr = chunk_rows[kind];
+            int64_t xoff = -1;
+            if (kind == kRowsCand) {
+                xoff = P.n_full;
+                P.tasks.push_back(ExpandTask{s, block, xoff});
+                P.n_full += (int64_t)S.n_spin;
+            }
             for (int64_t b = 0; b < count; b += cr) {
                 BatchChunk c{};
                 c.sec = s;
                 c.block = block;
                 c.begin = start + b;
                 c.end = start + std::min<int64_t>(count, b + cr);
+                c.xoff = xoff;
                 by_kind[kind].push_back((int)P.chunks.size());
                 P.chunks.push_back(c);
             }
@@ -391,6 +400,9 @@ static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, int c
     if (int rc = step_hv_free(dtype, minb, a, st)) return rc;
     a.idx = idx0 + kind_first[kRowsCand];
     a.count = kind_count[kRowsCand];
+    if (a.count > 0 && a.ntasks > 0) {
+        if (int rc = step_expand(dtype, a, st)) return rc;
+    }
     a.grid = dtype == ED_F32 ? cand_grid_f32 : other_grid;
     if (int rc = step_hv_cand(dtype, a, st)) return rc;
     a.grid = other_grid;
@@ -427,9 +439,14 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     DevBuf<int> dcfirst(nsec), dccount(nsec);
     DevBuf<double> partials((int64_t)nchunks * kReduceSlots);
     DevBuf<uint8_t> buf0((int64_t)(total * esz)), buf1((int64_t)(total * esz));
+    const int ntasks = (int)plan.tasks.size();
+    DevBuf<ExpandTask> dtasks(ntasks);
+    DevBuf<uint8_t> xfull((int64_t)(plan.n_full * (int64_t)esz));
     if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dkidx.ok() || !dcfirst.ok() || !dccount.ok() ||
-        !partials.ok() || !buf0.ok() || !buf1.ok())
+        !partials.ok() || !buf0.ok() || !buf1.ok() || !dtasks.ok() || !xfull.ok())
         return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
+    if (ntasks)
+        cudaMemcpyAsync(dtasks.p, plan.tasks.data(), ntasks * sizeof(ExpandTask), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doffs.p, hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dchunks.p, plan.chunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
@@ -466,7 +483,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
         StepArgs a{dviews.p, doffs.p, dchunks.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
-                    partials.p};
+                    partials.p, dtasks.p, ntasks, (int64_t)s0.n_spin, xfull.p};
         if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid, s0.cand_grid_f32,
                                  plan.kind_first, plan.kind_count, a, cap)) {
             if (use_graph) {
@@ -554,6 +571,16 @@ int single_setup(Sector& s) {
     cudaMemcpy(s.d_ccount.p, plan.ccount.data(), sizeof(int), cudaMemcpyHostToDevice);
     if (!s.d_partials.alloc((int64_t)(count > 0 ? count : 1) * kReduceSlots))
         return set_error(ED_ERR_NOMEM, "sector reduction scratch");
+    // stabiliser blocks' expanded copies: allocated here, once, for the widest element (complex
+    // double, which a real sector also accepts), so that no step allocates (steps may be captured
+    // in a CUDA graph)
+    s.n_tasks = (int)plan.tasks.size();
+    s.n_full = plan.n_full;
+    if (s.n_tasks > 0) {
+        if (!s.d_tasks.alloc(s.n_tasks) || !s.d_xfull.alloc(s.n_full * 16))
+            return set_error(ED_ERR_NOMEM, "sector expansion scratch");
+        cudaMemcpy(s.d_tasks.p, plan.tasks.data(), s.n_tasks * sizeof(ExpandTask), cudaMemcpyHostToDevice);
+    }
     return ED_OK;
 }
 
@@ -569,7 +596,8 @@ template <typename R, bool CPLX>
 static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
                            double* scal, cudaStream_t st) {
     StepArgs a{s.d_self.p, s.d_offs.p, s.d_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
-               const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p};
+               const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p,
+               s.d_tasks.p, s.n_tasks, (int64_t)s.n_spin, s.d_xfull.p};
     if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.hv_grid, s.other_grid, s.cand_grid_f32, s.kind_first,
                              s.kind_count, a, st))
         return rc;

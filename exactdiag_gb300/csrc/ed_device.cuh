@@ -611,85 +611,18 @@ __device__ __forceinline__ void block_hops(const SectorView& S, const HvTables<R
     }
 }
 
-// A stabiliser of two elements {identity, g} (cand[0], cand[1] of a block with ncand == 2), with
-// the images under g of every bond flip built once per chunk (build_pair_stab): an exchange
-// target's image is then g(dc) ^ g(flip).
-struct PairStab {
-    uint32_t gf1[32];  // g(1 << a | 1 << (a + 1))
-    uint32_t gf2[32];  // g(1 << a | 1 << (a + 2))
-    uint32_t gfw[2];   // g of the flips of the wrap bonds
-    int e0, eg;        // phase exponents of the identity and of g
-};
-
-// Threads 0..31 fill one position each (the caller synchronises).  Only for ncand == 2.
-__device__ __forceinline__ void build_pair_stab(const BlockDesc& D, int Ns, PairStab& P) {
-    const int a = threadIdx.x;
-    if (a < 32) {
-        const CandParams& g = D.cand[1];
-        P.gf1[a] = a + 1 < Ns ? cand_image(g, (1u << a) | (2u << a), Ns) : 0u;
-        P.gf2[a] = a + 2 < Ns ? cand_image(g, (1u << a) | (4u << a), Ns) : 0u;
-        if (a < 2) P.gfw[a] = a < D.nwrap ? cand_image(g, (1u << D.wrap[a][0]) | (1u << D.wrap[a][1]), Ns) : 0u;
-        if (a == 0) {
-            P.e0 = D.cand[0].e;
-            P.eg = g.e;
-        }
-    }
-}
-
-// Exchange terms of a row of a block whose stabiliser is {identity, g}: the target t = dc ^ flip
-// and its image g(t) = g(dc) ^ g(flip) (the flip's image from P); the lower of the two is the
-// representative, t == g(t) halves the orbit and needs the phases of identity and g to agree
-// (the reference's amplitude test, symmetry_ladder.h:196-224), then the bitmap gives its row.
-template <typename R, bool CPLX>
-__device__ __forceinline__ void pair_exchange(const SectorView& S, const HvTables<R>& tb, const PairStab& P,
-                                              const CandParams& g, int64_t word_off, uint32_t dc, uint32_t mr,
-                                              uint32_t ma, uint32_t m2, uint32_t wrap_anti, const int (&wlo)[2],
-                                              const int (&whi)[2], R cr, R cl, int Ns, int N,
-                                              const void* __restrict__ x, R& accr, R& acci) {
-    const uint32_t gx = cand_image(g, dc, Ns);
-    const R rN = tb.rsqrtv[N], rN2 = tb.rsqrtv[N >> 1];
-    const int e0 = P.e0, eg = P.eg;
-    const bool phases_agree = e0 == eg;
-#pragma unroll 1
-    for (int kind = 0; kind < 4; ++kind) {
-        uint32_t m;
-        int dist;
-        R coef;
-        const uint32_t* gtab;
-        if (kind == 0) { m = mr; dist = 1; coef = cr; gtab = P.gf1; }
-        else if (kind == 1) { m = ma; dist = 1; coef = cl; gtab = P.gf1; }
-        else if (kind == 2) { m = m2; dist = 2; coef = cl; gtab = P.gf2; }
-        else { m = wrap_anti; dist = 0; coef = cl; gtab = P.gfw; }
-        if (coef == R(0)) continue;
-        const R c1 = coef * rN, c2 = coef * rN2;
-        while (m) {
-            const int a = 31 - __clz(m);
-            m ^= 1u << a;
-            const uint32_t flip = dist ? ((1u << a) | (1u << (a + dist)))
-                                       : ((1u << (a ? wlo[1] : wlo[0])) | (1u << (a ? whi[1] : whi[0])));
-            const uint32_t t = dc ^ flip, gt = gx ^ gtab[a];
-            const bool eq = gt == t;
-            if (eq && !phases_agree) continue;
-            const bool lower = gt < t;
-            const int64_t j = bitmap_row(S, word_off, spin_rank(lower ? gt : t, tb.rank, S.Nd));
-            if (j < 0) continue;
-            gather_add<R, CPLX>(x, j, eq ? c2 : c1, lower ? eg : e0, tb, accr, acci);
-        }
-    }
-}
-
 // Row i of H via the block descriptor D (the row's own block): free blocks move in dense-row
 // space directly (colex rank deltas), hops and non-free blocks go through the precomputed coset
 // permutations.  Rows of blocks marked generic take hv_row.
 // XIN: the caller has already loaded x_i into (xir, xii).
-// shop: the block's pre-built hops, pstab: its two-element stabiliser when ncand == 2 (both used
-// only by the kind-specialised rows, ROWS != 0).
+// shop: the block's pre-built hops (kind-specialised rows, ROWS != 0); xfull: the block's expanded
+// copy (ExpandTask), read by the stabiliser-row kernel (ROWS == kRowsCand).
 template <typename R, bool CPLX, int ROWS = 0, bool XIN = false>
 __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<R>& tb, const R w[4], int64_t i,
                                             uint64_t key, const BlockDesc* __restrict__ D,
                                             const void* __restrict__ x, R& outr, R& outi, R& xir, R& xii,
                                             const BlockHop<R>* __restrict__ shop = nullptr,
-                                            const PairStab* __restrict__ pstab = nullptr) {
+                                            const void* __restrict__ xfull = nullptr) {
     const uint32_t h = (uint32_t)(key >> 32), d = (uint32_t)key;
     const int Ns = S.Ns, N = S.N;
     if constexpr (!XIN) ld<R, CPLX>(x, i, xir, xii);
@@ -732,12 +665,16 @@ __device__ __forceinline__ void hv_row_fast(const SectorView& S, const HvTables<
         const int ncand = (dw1.x >> 16) & 255u;
         const int64_t word_off = D->word_off;
         const R cr = R(0.5) * wr * sqNi, cl = R(0.5) * wl * sqNi;
-        if (ROWS != 0 && ncand == 2) {
-            pair_exchange<R, CPLX>(S, tb, *pstab, D->cand[1], word_off, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, Ns,
-                                   N, x, accr, acci);
+        if constexpr (ROWS == kRowsCand) {
+            // the block's expanded copy holds every spin configuration's resolved value: its rows
+            // read exchange targets like a free block's, at the row's own colex rank +- delta
+            const typename Vec<R, CPLX>::T* xb = reinterpret_cast<const typename Vec<R, CPLX>::T*>(xfull);
+            const uint32_t rr = spin_rank(dc, tb.rank, S.Nd);
+            if (cr == cl) free_exchange<R, CPLX, true>(tb, xb, rr, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, S.Nd, accr, acci);
+            else free_exchange<R, CPLX, false>(tb, xb, rr, dc, mr, ma, m2, wrap_anti, wlo, whi, cr, cl, S.Nd, accr, acci);
         }
 #pragma unroll 1
-        for (int kind = 0; kind < (ROWS != 0 && ncand == 2 ? 0 : 4); ++kind) {
+        for (int kind = 0; kind < (ROWS == kRowsCand ? 0 : 4); ++kind) {
             uint32_t m;
             int dist;
             R coef;

@@ -87,6 +87,17 @@ struct BatchChunk {
     int32_t sec;
     int32_t block;       // descriptor of the chunk's block (every row of a chunk is in one block), or -1
     int64_t begin, end;  // rows of sector `sec`
+    int64_t xoff;        // stabiliser blocks: first element of the block's expanded copy (ExpandTask), else -1
+};
+
+// One stabiliser block of a step layout whose vector entries are expanded, every step, to all
+// C(Ns, Nd) spin configurations of its hole mask: out[r] for the configuration of colex rank r is
+// conj(u^e) x[rep] / sqrt(orbit) (0 for a configuration the sector's phases exclude), so that its
+// rows' exchange targets are read like a free block's (row rank +- delta).
+struct ExpandTask {
+    int32_t sec;
+    int32_t block;
+    int64_t out_off;  // first element of the block's copy in the step layout's expansion scratch
 };
 
 // Chunk tables of a step layout (one sector, or a batch of sectors): all chunks sector-major in
@@ -97,6 +108,8 @@ struct ChunkPlan {
     int kind_first[4] = {0, 0, 0, 0};
     int kind_count[4] = {0, 0, 0, 0};
     std::vector<int> cfirst, ccount;  // per sector
+    std::vector<ExpandTask> tasks;    // stabiliser blocks, in chunk order
+    int64_t n_full = 0;               // elements of the expansion scratch
 };
 
 struct Sector {
@@ -134,6 +147,12 @@ struct Sector {
     int kind_count[4] = {0, 0, 0, 0};
     DevBuf<int> d_cfirst, d_ccount;
     DevBuf<BlockDesc> d_desc;    // fast-row descriptors
+    // stabiliser blocks' expanded copies (single-sector steps): tasks and scratch for the widest
+    // element (16 bytes)
+    int n_tasks = 0;
+    int64_t n_full = 0;
+    DevBuf<ExpandTask> d_tasks;
+    DevBuf<uint8_t> d_xfull;
 };
 
 // ed_basis.cu
@@ -180,8 +199,14 @@ struct StepArgs {
     int stride;
     int k;
     double* partials;
+    // stabiliser blocks' expansion: tasks, their count, C(Ns, Nd), the scratch
+    const ExpandTask* tasks;
+    int ntasks;
+    int64_t n_spin;
+    void* xfull;
 };
 int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st);
+int step_expand(int dtype, const StepArgs& a, cudaStream_t st);
 int step_hv_cand(int dtype, const StepArgs& a, cudaStream_t st);
 int step_hv_generic(int dtype, const StepArgs& a, cudaStream_t st);
 int step_free_occupancy(int minb, size_t smem);

@@ -5,10 +5,10 @@
 //   y_i = (H v)_i - b_k v_{k-1,i}                    (general/cython_lanczos_diagonalization.pyx:68-77)
 // stores y_i, and accumulates the chunk's partial sums <v,Hv>, |y|^2, <v,y>, |v|^2 (per thread
 // exactly, see Accum; per chunk in FP64).  Every row of a chunk lies in one block, so the CTA
-// stages that block's descriptor once per chunk and builds from it what all its rows share: the
-// hop records (BlockHop) and, for a two-element stabiliser, the images of the bond flips
-// (PairStab).  Instantiations by row kind keep each kernel's register budget to the code its rows
-// need: free blocks never touch the coset or bitmap code of the others.
+// stages that block's descriptor once per chunk and builds from it the hop records all its rows
+// share (BlockHop).  Rows of stabiliser blocks read their exchange targets from the block's
+// expanded copy (expand_cand_kernel, run first in the step).  Instantiations by row kind keep each
+// kernel's register budget to the code its rows need.
 #pragma once
 
 #include "ed_device.cuh"
@@ -85,25 +85,24 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
     lanczos_hv_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                       const BatchChunk* __restrict__ chunks, const int* __restrict__ idx, int count, HvWeights W,
                       void* v, void* vprev, void* other, int first, const double* __restrict__ scal, int stride,
-                      int k, double* __restrict__ partials) {
+                      int k, double* __restrict__ partials, void* xfull) {
     extern __shared__ __align__(16) uint8_t smem[];
     const HvTables<R> tb = load_tables<R>(views[0], smem);
     const R w[4] = {(R)W.w[0], (R)W.w[1], (R)W.w[2], (R)W.w[3]};
     __shared__ __align__(16) BlockDesc sdesc;
     __shared__ BlockHop<R> shop[KIND == kRowsGeneric ? 1 : kMaxHops];
-    __shared__ PairStab pstab;
     for (int c = blockIdx.x; c < count; c += gridDim.x) {
         const int cid = idx[c];
         const BatchChunk ch = chunks[cid];
         const SectorView S = views[ch.sec];
         if constexpr (KIND != kRowsGeneric) {
-            // stage_block's first barrier also ends the previous chunk's reads of shop and pstab
+            // stage_block's first barrier also ends the previous chunk's reads of shop
             stage_block(S.desc + ch.block, &sdesc);
             build_block_hops<R, CPLX>(sdesc, tb, w, S.Ns, S.N, KIND == kRowsFree, shop);
-            if (KIND == kRowsCand && sdesc.ncand == 2) build_pair_stab(sdesc, S.Ns, pstab);
             __syncthreads();
         }
         const void* x = vec_at<R, CPLX>(v, offs[ch.sec]);
+        const void* xfull_b = KIND == kRowsCand ? vec_at<R, CPLX>(xfull, ch.xoff) : nullptr;
         void* y = vec_at<R, CPLX>(other, offs[ch.sec]);
         const void* yp = first ? nullptr : vec_at<R, CPLX>(vprev, offs[ch.sec]);
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
@@ -152,7 +151,7 @@ __global__ void __launch_bounds__(kHvThreads, MINB)
                     if (!first) ld<R, CPLX>(yp, in, pr_n, pi_n);
                 }
                 R hr, hi;
-                hv_row_fast<R, CPLX, KIND, true>(S, tb, w, i, key, &sdesc, x, hr, hi, xr, xi, shop, &pstab);
+                hv_row_fast<R, CPLX, KIND, true>(S, tb, w, i, key, &sdesc, x, hr, hi, xr, xi, shop, xfull_b);
                 finish_row(i, hr, hi, xr, xi, pr, pi);
                 key = key_n;
                 xr = xr_n;
@@ -178,8 +177,92 @@ inline int launch_step_kind(const StepArgs& a, cudaStream_t st) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.smem);
     const int grid = a.grid < a.count ? a.grid : a.count;
     kern<<<grid, kHvThreads, a.smem, st>>>(a.views, a.offs, a.chunks, a.idx, a.count, a.w, a.v, a.vprev, a.other,
-                                           a.first, a.scal, a.stride, a.k, a.partials);
+                                           a.first, a.scal, a.stride, a.k, a.partials, a.xfull);
     ED_CHECK_LAUNCH("lanczos_hv_kernel");
+    return ED_OK;
+}
+
+// ------------------------------------------------------------ stabiliser blocks' expanded copies
+
+constexpr int kExpandRun = 16;  // consecutive colex ranks per thread: one unrank, then next-combination steps
+constexpr int kExpandThreads = 256;
+
+// The Nd-bit mask of colex rank r among Ns bits (comb[k * kCombStride + n] = C(n, k)): the j-th set
+// bit from the top is the largest p with C(p, k) <= what remains of r, k counting down from Nd.
+__device__ __forceinline__ uint32_t colex_unrank(int64_t r, int Ns, int Nd, const uint32_t* comb) {
+    uint32_t m = 0;
+    int p = Ns - 1;
+    for (int k = Nd; k >= 1; --k) {
+        while ((int64_t)comb[k * kCombStride + p] > r) --p;
+        m |= 1u << p;
+        r -= comb[k * kCombStride + p];
+        --p;
+    }
+    return m;
+}
+
+// The next mask with the same number of set bits (next colex rank); v must not be the last one.
+__device__ __forceinline__ uint32_t next_combination(uint32_t v) {
+    const uint32_t t = v | (v - 1u);
+    return (t + 1u) | (((~t & (0u - ~t)) - 1u) >> __ffs(v));
+}
+
+// out[r] = conj(u^e) x[rep] / sqrt(orbit) for every spin configuration r of each task's block, as
+// the stabiliser rows' exchange terms read it (resolve_cand, bitmap_row and the phase rule of
+// gather_add, applied once per configuration instead of once per row and bond); 0 where the
+// sector's phases exclude the configuration.
+template <typename R, bool CPLX>
+__global__ void __launch_bounds__(kExpandThreads)
+    expand_cand_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
+                       const ExpandTask* __restrict__ tasks, int ntasks, int64_t n_spin, void* v, void* xfull) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const HvTables<R> tb = load_tables<R>(views[0], smem);
+    const int64_t runs = (n_spin + kExpandRun - 1) / kExpandRun;
+    const int64_t total = runs * ntasks;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int t = (int)(u / runs);
+        const int64_t r0 = (u - (int64_t)t * runs) * kExpandRun;
+        const int64_t r1 = r0 + kExpandRun < n_spin ? r0 + kExpandRun : n_spin;
+        const ExpandTask T = tasks[t];
+        const SectorView& S = views[T.sec];
+        const BlockDesc* D = S.desc + T.block;
+        const int ncand = D->ncand;
+        const int64_t word_off = D->word_off;
+        const void* x = vec_at<R, CPLX>(v, offs[T.sec]);
+        void* out = vec_at<R, CPLX>(xfull, T.out_off);
+        uint32_t cfg = colex_unrank(r0, S.Ns, S.Nd, tb.comb);
+        for (int64_t r = r0; r < r1; ++r) {
+            R vr = R(0), vi = R(0);
+            const CandResult c = resolve_cand<true>(D->cand, ncand, cfg, S.Ns);
+            if (c.valid) {
+                const int64_t j = bitmap_row(S, word_off, spin_rank(c.best, tb.rank, S.Nd));
+                if (j >= 0) {
+                    R xr, xi;
+                    ld<R, CPLX>(x, j, xr, xi);
+                    const R f = tb.rsqrtv[orbit_of_count(S.N, c.count)];
+                    if constexpr (CPLX) {
+                        const R pr = f * tb.cosv[c.e], pi = f * tb.sinv[c.e];
+                        vr = pr * xr - pi * xi;
+                        vi = pr * xi + pi * xr;
+                    } else {
+                        vr = (c.e == 0 ? f : -f) * xr;
+                    }
+                }
+            }
+            st<R, CPLX>(out, r, vr, vi);
+            if (r + 1 < r1) cfg = next_combination(cfg);
+        }
+    }
+}
+
+template <typename R, bool CPLX>
+inline int launch_expand(const StepArgs& a, cudaStream_t st, int num_sms) {
+    auto* kern = expand_cand_kernel<R, CPLX>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.smem);
+    const int64_t work = ((a.n_spin + kExpandRun - 1) / kExpandRun) * a.ntasks;
+    const int grid = grid_for(work, kExpandThreads, num_sms, 4);
+    kern<<<grid, kExpandThreads, a.smem, st>>>(a.views, a.offs, a.tasks, a.ntasks, a.n_spin, a.v, a.xfull);
+    ED_CHECK_LAUNCH("expand_cand_kernel");
     return ED_OK;
 }
 

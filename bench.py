@@ -40,7 +40,7 @@ METRIC = "Lanczos steps/s & HÂ·v HBM GB/s, 2Ã—14 t-J: mixed vs FP64 GPU at Î”Eâ‰
 UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
-KERNEL_VERSION = "v8"  # the H.v kernel generation the committed traffic figure was captured on
+KERNEL_VERSION = "v9"  # the H.v kernel generation the committed traffic figure was captured on
 
 
 def workload_name(sector) -> str:

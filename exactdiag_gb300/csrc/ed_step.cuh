@@ -185,6 +185,7 @@ inline int launch_step_kind(const StepArgs& a, cudaStream_t st) {
 // ------------------------------------------------------------ stabiliser blocks' expanded copies
 
 constexpr int kExpandRun = 16;  // consecutive colex ranks per thread: one unrank, then next-combination steps
+constexpr int kExpandBatch = 4;  // configurations of a run resolved together (loads in flight)
 constexpr int kExpandThreads = 256;
 
 // The Nd-bit mask of colex rank r among Ns bits (comb[k * kCombStride + n] = C(n, k)): the j-th set
@@ -231,26 +232,53 @@ __global__ void __launch_bounds__(kExpandThreads)
         const void* x = vec_at<R, CPLX>(v, offs[T.sec]);
         void* out = vec_at<R, CPLX>(xfull, T.out_off);
         uint32_t cfg = colex_unrank(r0, S.Ns, S.Nd, tb.comb);
-        for (int64_t r = r0; r < r1; ++r) {
-            R vr = R(0), vi = R(0);
-            const CandResult c = resolve_cand<true>(D->cand, ncand, cfg, S.Ns);
-            if (c.valid) {
-                const int64_t j = bitmap_row(S, word_off, spin_rank(c.best, tb.rank, S.Nd));
-                if (j >= 0) {
-                    R xr, xi;
-                    ld<R, CPLX>(x, j, xr, xi);
-                    const R f = tb.rsqrtv[orbit_of_count(S.N, c.count)];
-                    if constexpr (CPLX) {
-                        const R pr = f * tb.cosv[c.e], pi = f * tb.sinv[c.e];
-                        vr = pr * xr - pi * xi;
-                        vi = pr * xi + pi * xr;
-                    } else {
-                        vr = (c.e == 0 ? f : -f) * xr;
+        // kExpandBatch configurations at a time: their bitmap words, then their x, are in flight together
+        for (int64_t r = r0; r < r1; r += kExpandBatch) {
+            CandResult c[kExpandBatch];
+            uint32_t rk[kExpandBatch];
+            bool live[kExpandBatch];
+#pragma unroll
+            for (int u = 0; u < kExpandBatch; ++u) {
+                live[u] = false;
+                rk[u] = 0;
+                c[u] = CandResult{0u, 1, 0, false};
+                if (r + u < r1) {
+                    c[u] = resolve_cand<true>(D->cand, ncand, cfg, S.Ns);
+                    live[u] = c[u].valid;
+                    if (live[u]) rk[u] = spin_rank(c[u].best, tb.rank, S.Nd);
+                    if (r + u + 1 < r1) cfg = next_combination(cfg);
+                }
+            }
+            ulonglong2 bp[kExpandBatch];
+#pragma unroll
+            for (int u = 0; u < kExpandBatch; ++u)
+                if (live[u]) bp[u] = S.bitpref[word_off + (rk[u] >> 6)];
+            R xr[kExpandBatch], xi[kExpandBatch];
+#pragma unroll
+            for (int u = 0; u < kExpandBatch; ++u) {
+                xr[u] = xi[u] = R(0);
+                if (live[u]) {
+                    const uint64_t bit = 1ull << (rk[u] & 63u);
+                    if (bp[u].x & bit) {
+                        const int64_t j = (int64_t)bp[u].y + __popcll(bp[u].x & (bit - 1ull));
+                        ld<R, CPLX>(x, j, xr[u], xi[u]);
                     }
                 }
             }
-            st<R, CPLX>(out, r, vr, vi);
-            if (r + 1 < r1) cfg = next_combination(cfg);
+#pragma unroll
+            for (int u = 0; u < kExpandBatch; ++u) {
+                if (r + u >= r1) continue;
+                const R f = tb.rsqrtv[orbit_of_count(S.N, c[u].count)];
+                R vr, vi = R(0);
+                if constexpr (CPLX) {
+                    const R pr = f * tb.cosv[c[u].e], pi = f * tb.sinv[c[u].e];
+                    vr = pr * xr[u] - pi * xi[u];
+                    vi = pr * xi[u] + pi * xr[u];
+                } else {
+                    vr = (c[u].e == 0 ? f : -f) * xr[u];
+                }
+                st<R, CPLX>(out, r + u, vr, vi);
+            }
         }
     }
 }

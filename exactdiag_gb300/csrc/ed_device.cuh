@@ -376,11 +376,13 @@ __device__ __forceinline__ void gather_block(const typename Vec<R, CPLX>::T* __r
     }
 }
 
-// Exchange terms of a row of a free block: every neighbour is a representative of the same block
-// (orbit 2L, phase 1) at row ri +- delta, delta from the colex rank change of the swap.  Bonds
-// are taken from the highest bit down, one find-leading-one each, in counted loops unrolled by
-// four (independent gathers in flight per thread).  UNI (rung and leg exchange weights equal):
-// the x_j are summed with coefficient 1 and the sum scaled once; acc must be zero on entry.
+// Exchange terms of a row whose neighbours are read from xb at the row's colex rank ri +- delta,
+// delta the colex rank change of the swap: a free block's rows (every neighbour is a
+// representative of the same block, orbit 2L, phase 1, at that row offset), or a stabiliser
+// block's rows reading the block's expanded copy (ExpandTask).  Bonds are taken from the highest
+// bit down, one find-leading-one each, in counted loops unrolled by four (FP32) or two (FP64):
+// independent gathers in flight per thread.  UNI (rung and leg exchange weights equal): the x_j
+// are summed with coefficient 1 and the sum scaled once; acc must be zero on entry.
 template <typename R, bool CPLX, bool UNI>
 __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typename Vec<R, CPLX>::T* __restrict__ xb,
                                               uint32_t ri, uint32_t dc, uint32_t mr, uint32_t ma, uint32_t m2,
@@ -454,7 +456,7 @@ __device__ __forceinline__ void free_exchange(const HvTables<R>& tb, const typen
 // coefficient w * sign (times sqrt(2L) for rows of a free block, whose orbit is 2L; rows of a
 // stabiliser block multiply by sqrt of their own orbit).  For a free target the coefficient also
 // holds 1 / sqrt(2L) and the target's phase; for a stabiliser target the orbit and phase of the
-// target are resolved per row.
+// target are resolved per row (coset candidates and bitmap word).
 // Every field is a full word, read as four 16-byte words without unpacking.
 template <typename R>
 struct alignas(16) BlockHop {

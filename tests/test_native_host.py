@@ -1,0 +1,31 @@
+"""CPU: host-compiled checks of the descriptor builder (tests/native/*.cu), built with nvcc as host
+code -- no GPU is touched."""
+
+import pathlib
+import shutil
+import subprocess
+
+import pytest
+
+HERE = pathlib.Path(__file__).resolve().parent
+CSRC = HERE.parent / "exactdiag_gb300" / "csrc"
+
+
+def _nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not pathlib.Path(exe).exists():
+        pytest.skip("nvcc not available")
+    return exe
+
+
+def test_coset_phases_compose_with_the_stabiliser(tmp_path):
+    """Resolving through a hole mask's coset equals mapping by its first element and resolving with
+    the canonical mask's stabiliser, phases added (L = 4..8, 1-4 holes, every momentum)."""
+    exe = tmp_path / "coset_phase_check"
+    build = subprocess.run([_nvcc(), "-std=c++17", "--expt-relaxed-constexpr", "-O2", f"-I{CSRC}",
+                            f"-I{HERE.parent / 'include'}", str(HERE / "native" / "coset_phase_check.cu"), "-o", str(exe)],
+                           capture_output=True, text=True, timeout=600)
+    assert build.returncode == 0, build.stderr[-3000:]
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert run.returncode == 0, run.stdout[-3000:]
+    assert "differences 0" in run.stdout

@@ -219,6 +219,27 @@ __host__ __device__ __forceinline__ uint32_t spin_rank(uint32_t dc, const RankTa
     return r;
 }
 
+// The Nd-bit mask of colex rank r among Ns bits (comb[k * kCombStride + n] = C(n, k)): the j-th set
+// bit from the top is the largest p with C(p, k) <= what remains of r, k counting down from Nd.
+__host__ __device__ __forceinline__ uint32_t colex_unrank(int64_t r, int Ns, int Nd, const uint32_t* comb) {
+    uint32_t m = 0;
+    int p = Ns - 1;
+    for (int k = Nd; k >= 1; --k) {
+        while ((int64_t)comb[k * kCombStride + p] > r) --p;
+        m |= 1u << p;
+        r -= comb[k * kCombStride + p];
+        --p;
+    }
+    return m;
+}
+
+// The next mask with the same number of set bits (next colex rank); v must be non-zero and not the
+// last such mask below 2^32.
+__host__ __device__ __forceinline__ uint32_t next_combination(uint32_t v) {
+    const uint32_t t = v | (v - 1u);
+    return (t + 1u) | (((~t & (0u - ~t)) - 1u) >> (ctz32(v) + 1));
+}
+
 // RankTab over a copy T of the sector's rank tables.
 __host__ __device__ __forceinline__ RankTab rank_tab_of(const SectorView& S, const uint32_t* T) {
     RankTab rt;

@@ -155,6 +155,44 @@ struct Sector {
     DevBuf<uint8_t> d_xfull;
 };
 
+// Colex spin-rank tables of Ns spins with Nd down (layout: RankTab): fills V's rk_* fields and
+// rank_words and the table words.  comb[k][n] = C(n, k).  Host code, shared by ed_sector_create
+// and the host checks of the tables.
+inline void rank_tables_build(int Ns, int Nd, const uint32_t (&comb)[kCombStride][kCombStride], SectorView& V,
+                              std::vector<uint32_t>& tab) {
+    // chunk 0 of w0 bits (2^w0 entries, no set bits below it), then 8-bit chunks of Nd + 1 rows
+    const int nch = Ns <= 28 ? 3 : 4;
+    int w0 = Ns - 8 * (nch - 1);
+    if (w0 < 0) w0 = 0;
+    V.rk_nch = (uint32_t)nch;
+    V.rk_m0 = (1u << w0) - 1u;
+    uint32_t words = 1u << w0;
+    for (int c = 0; c < 4; ++c) {
+        V.rk_pos[c] = c == 0 ? 0u : (uint32_t)(w0 + 8 * (c - 1));
+        V.rk_off[c] = c == 0 ? 0u : words;
+        if (c > 0 && c < nch) words += (uint32_t)(Nd + 1) << 8;
+    }
+    V.rank_words = (int)words;
+    tab.assign(words, 0u);
+    auto chunk_sum = [&](uint32_t bits, int pos, int k) {
+        // sum over the set bits of `bits` (j-th from the bottom, at pos + b) of C(pos + b, k + j)
+        uint32_t r = 0;
+        int j = 0;
+        for (int b = 0; b < 16; ++b)
+            if (bits & (1u << b)) {
+                ++j;
+                const int nn = pos + b, kk = k + j;
+                if (nn <= kMaxN && kk <= kMaxN) r += comb[kk][nn];
+            }
+        return r;
+    };
+    for (uint32_t bits = 0; bits < (1u << w0); ++bits) tab[bits] = chunk_sum(bits, 0, 0);
+    for (int c = 1; c < nch; ++c)
+        for (int k = 0; k <= Nd; ++k)
+            for (uint32_t byte = 0; byte < 256u; ++byte)
+                tab[V.rk_off[c] + ((uint32_t)k << 8) + byte] = chunk_sum(byte, (int)V.rk_pos[c], k);
+}
+
 // ed_basis.cu
 int basis_build(Sector& s, cudaStream_t st);
 int basis_export(Sector& s, int64_t* sparse_dev, int32_t* orbit_dev, cudaStream_t st);

@@ -188,26 +188,6 @@ constexpr int kExpandRun = 16;  // consecutive colex ranks per thread: one unran
 constexpr int kExpandBatch = 4;  // configurations of a run resolved together (loads in flight)
 constexpr int kExpandThreads = 256;
 
-// The Nd-bit mask of colex rank r among Ns bits (comb[k * kCombStride + n] = C(n, k)): the j-th set
-// bit from the top is the largest p with C(p, k) <= what remains of r, k counting down from Nd.
-__device__ __forceinline__ uint32_t colex_unrank(int64_t r, int Ns, int Nd, const uint32_t* comb) {
-    uint32_t m = 0;
-    int p = Ns - 1;
-    for (int k = Nd; k >= 1; --k) {
-        while ((int64_t)comb[k * kCombStride + p] > r) --p;
-        m |= 1u << p;
-        r -= comb[k * kCombStride + p];
-        --p;
-    }
-    return m;
-}
-
-// The next mask with the same number of set bits (next colex rank); v must not be the last one.
-__device__ __forceinline__ uint32_t next_combination(uint32_t v) {
-    const uint32_t t = v | (v - 1u);
-    return (t + 1u) | (((~t & (0u - ~t)) - 1u) >> __ffs(v));
-}
-
 // out[r] = conj(u^e) x[rep] / sqrt(orbit) for every spin configuration r of each task's block, as
 // the stabiliser rows' exchange terms read it (resolve_cand, bitmap_row and the phase rule of
 // gather_add, applied once per configuration instead of once per row and bond); 0 where the

@@ -18,14 +18,25 @@ def _nvcc() -> str:
     return exe
 
 
-def test_coset_phases_compose_with_the_stabiliser(tmp_path):
-    """Resolving through a hole mask's coset equals mapping by its first element and resolving with
-    the canonical mask's stabiliser, phases added (L = 4..8, 1-4 holes, every momentum)."""
-    exe = tmp_path / "coset_phase_check"
+def _build_and_run(tmp_path, name: str) -> str:
+    exe = tmp_path / name
     build = subprocess.run([_nvcc(), "-std=c++17", "--expt-relaxed-constexpr", "-O2", f"-I{CSRC}",
-                            f"-I{HERE.parent / 'include'}", str(HERE / "native" / "coset_phase_check.cu"), "-o", str(exe)],
+                            f"-I{HERE.parent / 'include'}", str(HERE / "native" / f"{name}.cu"), "-o", str(exe)],
                            capture_output=True, text=True, timeout=600)
     assert build.returncode == 0, build.stderr[-3000:]
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert run.returncode == 0, run.stdout[-3000:]
     assert "differences 0" in run.stdout
+    return run.stdout
+
+
+def test_coset_phases_compose_with_the_stabiliser(tmp_path):
+    """Resolving through a hole mask's coset equals mapping by its first element and resolving with
+    the canonical mask's stabiliser, phases added (L = 4..8, 1-4 holes, every momentum)."""
+    _build_and_run(tmp_path, "coset_phase_check")
+
+
+def test_rank_tables_unrank_and_next_combination(tmp_path):
+    """The spin-rank tables of every (Ns, Nd) give the colex rank; unranking and the
+    next-combination step of the stabiliser expansion invert and advance it."""
+    _build_and_run(tmp_path, "rank_tables_check")

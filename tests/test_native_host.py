@@ -20,7 +20,8 @@ def _nvcc() -> str:
 
 def _build_and_run(tmp_path, name: str) -> str:
     exe = tmp_path / name
-    build = subprocess.run([_nvcc(), "-std=c++17", "--expt-relaxed-constexpr", "-O2", f"-I{CSRC}",
+    build = subprocess.run([_nvcc(), "-std=c++17", "--expt-relaxed-constexpr", "-O2",
+                            "-gencode", "arch=compute_103a,code=sm_103a", f"-I{CSRC}",
                             f"-I{HERE.parent / 'include'}", str(HERE / "native" / f"{name}.cu"), "-o", str(exe)],
                            capture_output=True, text=True, timeout=600)
     assert build.returncode == 0, build.stderr[-3000:]
@@ -40,3 +41,10 @@ def test_rank_tables_unrank_and_next_combination(tmp_path):
     """The spin-rank tables of every (Ns, Nd) give the colex rank; unranking and the
     next-combination step of the stabiliser expansion invert and advance it."""
     _build_and_run(tmp_path, "rank_tables_check")
+
+
+def test_chunk_plan_cuts_each_sector_the_same_alone_and_batched(tmp_path):
+    """plan_chunks on synthetic sectors: chunks tile the rows inside their blocks with the per-kind
+    lengths, a sector is cut identically alone and in a batch, stabiliser chunks point at their
+    block's expanded copy."""
+    _build_and_run(tmp_path, "chunk_plan_check")

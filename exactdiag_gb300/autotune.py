@@ -22,7 +22,7 @@ import torch
 from exactdiag_gb300 import _native as nat
 from exactdiag_gb300.engine import DeviceSector
 
-CANDIDATES = ((3, 0), (4, 0), (3, 2), (4, 3))
+CANDIDATES = ((2, 0), (3, 0), (4, 0), (2, 1))
 
 
 def cache_path() -> pathlib.Path:

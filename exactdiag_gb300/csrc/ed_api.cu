@@ -128,7 +128,7 @@ int ed_basis_build(ed_sector* h, void* stream) {
     s.hv_grid = s.num_sms * per_sm;
     if (int rc2 = build_descriptors(s)) return rc2;
     if (int rc3 = single_setup(s)) return rc3;
-    return set_launch(s, 3, 0);
+    return set_launch(s, 2, 0);
 }
 
 int ed_sector_set_launch(ed_sector* h, int min_ctas_per_sm, int ctas_per_sm) {

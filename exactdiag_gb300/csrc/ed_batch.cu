@@ -331,24 +331,37 @@ __global__ void __launch_bounds__(kUpdThreads, 4)
     }
 }
 
-// Chunks of every sector: each block's rows cut every chunk_rows[kind] (a chunk never straddles
-// two blocks), sector-major in row order; the chunk ids grouped by row kind.  A kind's chunks are
-// kChunkRows long, halved (down to kChunkRows / 8) while the sector's rows of that kind would
-// make fewer chunks than four per SM, so that small kinds still spread over the whole GPU.  The
-// lengths depend on the sector alone: a sector is cut the same way alone and in a batch, so its
-// per-chunk sums, and with them its recursion, are the same bits either way.
+// Chunks of every sector.  Row chunks: each block's rows cut every chunk_rows[kind] (a chunk never
+// straddles two blocks), sector-major in row order; a kind's chunks are kChunkRows long, halved (down
+// to kChunkRows / 8) while the sector's rows of that kind would make fewer chunks than four per SM.
+// H.v chunks: for a free block, its segments class by class (kl = 0 .. P), about kSegChunkRows rows
+// per chunk in whole rounds of the segment kernel's slots; for the other blocks, their row chunks.
+// Both depend on the sector alone: a sector is cut the same way alone and in a batch, so its
+// per-chunk sums, and with them its recursion, are the same bits either way.  Expanded copies: one
+// per block of Sector::copy_blocks, sector by sector.
 void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
     const int nsec = (int)secs.size();
     P.chunks.clear();
+    P.hv.clear();
     P.kind_idx.clear();
     P.cfirst.assign(nsec, 0);
     P.ccount.assign(nsec, 0);
+    P.hv_first.assign(nsec, 0);
+    P.hv_count.assign(nsec, 0);
     P.tasks.clear();
     P.n_full = 0;
     std::vector<int> by_kind[4];
     for (int s = 0; s < nsec; ++s) {
         const Sector& S = *secs[s];
         P.cfirst[s] = (int)P.chunks.size();
+        P.hv_first[s] = (int)P.hv.size();
+        const int64_t copy_base = P.n_full;
+        std::vector<int64_t> copy_off(S.view.n_blocks > 0 ? S.view.n_blocks : 1, -1);
+        for (int b : S.copy_blocks) {
+            copy_off[b] = P.n_full;
+            P.tasks.push_back(ExpandTask{s, b, P.n_full});
+            P.n_full += (int64_t)S.n_spin;
+        }
         int64_t kind_rows[4] = {0, 0, 0, 0};
         if (S.spans.empty()) kind_rows[kRowsGeneric] += S.view.n;
         for (const BlockSpan& sp : S.spans) kind_rows[sp.kind] += sp.count;
@@ -360,12 +373,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
         }
         auto add_span = [&](int64_t start, int64_t count, int block, int kind) {
             const int64_t cr = chunk_rows[kind];
-            int64_t xoff = -1;
-            if (kind == kRowsCand) {
-                xoff = P.n_full;
-                P.tasks.push_back(ExpandTask{s, block, xoff});
-                P.n_full += (int64_t)S.n_spin;
-            }
+            const int64_t xoff = kind == kRowsCand ? copy_off[block] : -1;
             for (int64_t b = 0; b < count; b += cr) {
                 BatchChunk c{};
                 c.sec = s;
@@ -373,14 +381,42 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
                 c.begin = start + b;
                 c.end = start + std::min<int64_t>(count, b + cr);
                 c.xoff = xoff;
-                by_kind[kind].push_back((int)P.chunks.size());
+                c.kl = -1;
                 P.chunks.push_back(c);
+                if (kind != kRowsFree) {
+                    by_kind[kind].push_back((int)P.hv.size());
+                    P.hv.push_back(c);
+                }
+            }
+            if (kind != kRowsFree) return;
+            // segment chunks of a free block
+            const int Pb = S.view.seg_p;
+            for (int kl = 0; kl <= Pb; ++kl) {
+                const int64_t nseg = (int64_t)S.host_seg_off[kl + 1] - (int64_t)S.host_seg_off[kl];
+                if (nseg <= 0) continue;
+                int64_t nA = 1;  // C(Pb, kl)
+                for (int j = 1; j <= kl; ++j) nA = nA * (Pb - kl + j) / j;
+                const int64_t slots = std::min<int64_t>(kSegSlots, (kSegThreads - 1) / nA);
+                const int64_t rounds = std::max<int64_t>(1, kSegChunkRows / (nA * slots));
+                const int64_t per = slots * rounds;
+                for (int64_t g = 0; g < nseg; g += per) {
+                    BatchChunk c{};
+                    c.sec = s;
+                    c.block = block;
+                    c.begin = g;
+                    c.end = std::min<int64_t>(nseg, g + per);
+                    c.xoff = copy_base;
+                    c.kl = kl;
+                    by_kind[kRowsFree].push_back((int)P.hv.size());
+                    P.hv.push_back(c);
+                }
             }
         };
         if (S.spans.empty()) add_span(0, S.view.n, -1, kRowsGeneric);
         for (const BlockSpan& sp : S.spans)
             if (sp.count > 0) add_span(sp.start, sp.count, sp.block, sp.kind);
         P.ccount[s] = (int)P.chunks.size() - P.cfirst[s];
+        P.hv_count[s] = (int)P.hv.size() - P.hv_first[s];
     }
     for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind) {
         P.kind_first[kind] = (int)P.kind_idx.size();
@@ -394,15 +430,16 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
 static int step_hv_all(int dtype, int minb, int free_grid, int other_grid, int cand_grid_f32, const int kind_first[4],
                        const int kind_count[4], StepArgs a, cudaStream_t st) {
     const int* idx0 = a.idx;
+    // the expanded copies first: hops out of free blocks and the stabiliser rows read them
+    if (a.ntasks > 0) {
+        if (int rc = step_expand(dtype, a, st)) return rc;
+    }
     a.idx = idx0 + kind_first[kRowsFree];
     a.count = kind_count[kRowsFree];
     a.grid = free_grid;
     if (int rc = step_hv_free(dtype, minb, a, st)) return rc;
     a.idx = idx0 + kind_first[kRowsCand];
     a.count = kind_count[kRowsCand];
-    if (a.count > 0 && a.ntasks > 0) {
-        if (int rc = step_expand(dtype, a, st)) return rc;
-    }
     a.grid = dtype == ED_F32 ? cand_grid_f32 : other_grid;
     if (int rc = step_hv_cand(dtype, a, st)) return rc;
     a.grid = other_grid;
@@ -431,28 +468,34 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         total += hviews[s].n;
     }
     const int nchunks = (int)plan.chunks.size();
+    const int nhv = (int)plan.hv.size();
     const int stride = 2 * m + 4;
     DevBuf<SectorView> dviews(nsec);
     DevBuf<int64_t> doffs(nsec);
-    DevBuf<BatchChunk> dchunks(nchunks);
-    DevBuf<int> dkidx(nchunks);
-    DevBuf<int> dcfirst(nsec), dccount(nsec);
-    DevBuf<double> partials((int64_t)nchunks * kReduceSlots);
+    DevBuf<BatchChunk> dchunks(nchunks), dhv(nhv);
+    DevBuf<int> dkidx(nhv);
+    DevBuf<int> dcfirst(nsec), dccount(nsec), dhfirst(nsec), dhcount(nsec);
+    DevBuf<double> partials((int64_t)std::max(nchunks, nhv) * kReduceSlots);
     DevBuf<uint8_t> buf0((int64_t)(total * esz)), buf1((int64_t)(total * esz));
     const int ntasks = (int)plan.tasks.size();
     DevBuf<ExpandTask> dtasks(ntasks);
     DevBuf<uint8_t> xfull((int64_t)(plan.n_full * (int64_t)esz));
-    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dkidx.ok() || !dcfirst.ok() || !dccount.ok() ||
-        !partials.ok() || !buf0.ok() || !buf1.ok() || !dtasks.ok() || !xfull.ok())
+    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dhv.ok() || !dkidx.ok() || !dcfirst.ok() || !dccount.ok() ||
+        !dhfirst.ok() || !dhcount.ok() || !partials.ok() || !buf0.ok() || !buf1.ok() || !dtasks.ok() || !xfull.ok())
         return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
     if (ntasks)
         cudaMemcpyAsync(dtasks.p, plan.tasks.data(), ntasks * sizeof(ExpandTask), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doffs.p, hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dchunks.p, plan.chunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dkidx.p, plan.kind_idx.data(), nchunks * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (nhv) {
+        cudaMemcpyAsync(dhv.p, plan.hv.data(), nhv * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dkidx.p, plan.kind_idx.data(), nhv * sizeof(int), cudaMemcpyHostToDevice, st);
+    }
     cudaMemcpyAsync(dcfirst.p, plan.cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dccount.p, plan.ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dhfirst.p, plan.hv_first.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dhcount.p, plan.hv_count.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(coef, 0, (size_t)nsec * stride * sizeof(double), st);
     for (int s = 0; s < nsec; ++s)
         if (hviews[s].n)
@@ -482,7 +525,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
     for (int k = 0; k < m; ++k) {
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
-        StepArgs a{dviews.p, doffs.p, dchunks.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
+        StepArgs a{dviews.p, doffs.p, dhv.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
                     partials.p, dtasks.p, ntasks, (int64_t)s0.n_spin, xfull.p};
         if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid, s0.cand_grid_f32,
                                  plan.kind_first, plan.kind_count, a, cap)) {
@@ -494,7 +537,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
             }
             return rc;
         }
-        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 0, 0);
+        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dhfirst.p, dhcount.p, coef, stride, k, 0, 0);
         lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
                                                                       stride, k, 0, 0);
         // sectors whose b needs the exact norm: y - a v and its norm, b, then v_{k+1} /= b
@@ -553,24 +596,30 @@ int single_setup(Sector& s) {
     plan_chunks({&s}, plan);
     const int64_t zero = 0;
     const int count = (int)plan.chunks.size();
+    const int nhv = (int)plan.hv.size();
     s.n_chunks = count;
+    s.n_hv_chunks = nhv;
     for (int kind = 0; kind < 4; ++kind) {
         s.kind_first[kind] = plan.kind_first[kind];
         s.kind_count[kind] = plan.kind_count[kind];
     }
     if (!s.d_self.alloc(1) || !s.d_offs.alloc(1) || !s.d_chunks.alloc(count > 0 ? count : 1) ||
-        !s.d_kidx.alloc(count > 0 ? count : 1) || !s.d_cfirst.alloc(1) || !s.d_ccount.alloc(1))
+        !s.d_hv_chunks.alloc(nhv > 0 ? nhv : 1) || !s.d_kidx.alloc(nhv > 0 ? nhv : 1) || !s.d_cfirst.alloc(1) ||
+        !s.d_ccount.alloc(1) || !s.d_hv_first.alloc(1) || !s.d_hv_count.alloc(1))
         return set_error(ED_ERR_NOMEM, "sector step tables");
     cudaMemcpy(s.d_self.p, &s.view, sizeof(SectorView), cudaMemcpyHostToDevice);
     cudaMemcpy(s.d_offs.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice);
-    if (count) {
-        cudaMemcpy(s.d_chunks.p, plan.chunks.data(), count * sizeof(BatchChunk), cudaMemcpyHostToDevice);
-        cudaMemcpy(s.d_kidx.p, plan.kind_idx.data(), count * sizeof(int), cudaMemcpyHostToDevice);
+    if (count) cudaMemcpy(s.d_chunks.p, plan.chunks.data(), count * sizeof(BatchChunk), cudaMemcpyHostToDevice);
+    if (nhv) {
+        cudaMemcpy(s.d_hv_chunks.p, plan.hv.data(), nhv * sizeof(BatchChunk), cudaMemcpyHostToDevice);
+        cudaMemcpy(s.d_kidx.p, plan.kind_idx.data(), nhv * sizeof(int), cudaMemcpyHostToDevice);
     }
     cudaMemcpy(s.d_cfirst.p, plan.cfirst.data(), sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(s.d_ccount.p, plan.ccount.data(), sizeof(int), cudaMemcpyHostToDevice);
-    if (!s.d_partials.alloc((int64_t)(count > 0 ? count : 1) * kReduceSlots))
-        return set_error(ED_ERR_NOMEM, "sector reduction scratch");
+    cudaMemcpy(s.d_hv_first.p, plan.hv_first.data(), sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(s.d_hv_count.p, plan.hv_count.data(), sizeof(int), cudaMemcpyHostToDevice);
+    const int slots = std::max(std::max(count, nhv), 1);
+    if (!s.d_partials.alloc((int64_t)slots * kReduceSlots)) return set_error(ED_ERR_NOMEM, "sector reduction scratch");
     // stabiliser blocks' expanded copies: allocated here, once, for the widest element (complex
     // double, which a real sector also accepts), so that no step allocates (steps may be captured
     // in a CUDA graph)
@@ -595,13 +644,14 @@ static int step_grid(const Sector& s) { return update_grid(s, s.n_chunks); }
 template <typename R, bool CPLX>
 static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, const void* vprev, void* vnext,
                            double* scal, cudaStream_t st) {
-    StepArgs a{s.d_self.p, s.d_offs.p, s.d_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
+    StepArgs a{s.d_self.p, s.d_offs.p, s.d_hv_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
                const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p,
                s.d_tasks.p, s.n_tasks, (int64_t)s.n_spin, s.d_xfull.p};
     if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.hv_grid, s.other_grid, s.cand_grid_f32, s.kind_first,
                              s.kind_count, a, st))
         return rc;
-    lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_cfirst.p, s.d_ccount.p, scal, 0, 0, 0, 0);
+    lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_hv_first.p, s.d_hv_count.p, scal, 0, 0, 0,
+                                                         0);
     ED_CHECK_LAUNCH("lanczos_scalars_kernel");
     return ED_OK;
 }
@@ -609,7 +659,7 @@ static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, c
 // Launch shape of the step kernels: the free-row kernel's register variant (3 or 4 resident CTAs
 // per SM) and CTAs per SM (0 = as many as fit); the other kinds run as many CTAs as fit.
 int set_launch(Sector& s, int minb, int ctas_per_sm) {
-    if (minb != 3 && minb != 4) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: variant must be 3 or 4");
+    if (minb < 2 || minb > 4) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: variant must be 2, 3 or 4");
     if (ctas_per_sm < 0 || ctas_per_sm > 8) return set_error(ED_ERR_INVALID, "ed_sector_set_launch: ctas_per_sm");
     const size_t smem = hv_smem_bytes(s.view, sizeof(float));
     const int occ = step_free_occupancy(minb, smem);

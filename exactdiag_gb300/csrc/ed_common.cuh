@@ -108,6 +108,55 @@ struct alignas(16) BlockDesc {
 static_assert(offsetof(HopDesc, start) == 16 && offsetof(HopDesc, a) == 32, "HopDesc hot words");
 static_assert(offsetof(BlockDesc, mode) == 16 && offsetof(BlockDesc, start) == 24, "BlockDesc hot words");
 
+// ---- segment layout of free blocks (ed_seg.cuh) ------------------------------------------------
+//
+// The compressed down mask dc of a free block's row splits at position P = min(kSegA, Ns) into a
+// low part (bits [0, P)) and a high part H (bits [P, Ns)); the rows sharing H are contiguous (a
+// segment).  SegDesc lists a free block's terms by where their bits lie relative to P.
+
+constexpr int kSegA = 9;      // low compressed bits resolved per thread: C(9, k) <= 126 rows per segment
+constexpr int kSegMaxA = 16;  // exchange bonds with both ends below P
+constexpr int kSegMaxB = 48;  // exchange bonds with both ends at or above P
+constexpr int kSegMaxX = 8;   // exchange bonds across P
+
+// A hop as a permutation pi of compressed masks (move of the electron, then the target's coset
+// permutation: mirror pairs and rotation), classified by how it maps [0, P): nb of the P low
+// positions land at or above P (at bpos[0] < bpos[1]), and as many high positions land below P;
+// nb = 3 stands for "more than two" (the target rank is then taken per row).
+struct SegHopDesc {
+    uint32_t keep, band, swap;     // bits kept in place, bits shifted by one toward p, mirror pairs
+    uint8_t sl, sr, p, q;          // moved = ((x & band) << sl) >> sr; the electron goes from p to q
+    uint8_t rot, nsr, term, sign;  // left rotation by rot (nsr = (Ns - rot) % 32); 0 tl / 1 tr; 1: coefficient -w
+    uint8_t e, kind, nb, pad;      // phase exponent; 0 free target, 1 stabiliser target, 3 absent
+    uint8_t bpos[2], pad2[2];
+    int32_t tblock;                // target block
+    int64_t tstart;                // free target: its first row; stabiliser target: the index of its
+                                   // expanded copy among the sector's copies
+};
+
+// Per segment of a free block, a record of rec_len 32-bit words (built once per sector by
+// seg_records_kernel; the values depend on the segment's high part only, never on a vector):
+//   [0] the segment's first row in the block;  [1] nb | nbr << 8 | hib << 16;
+//   [2, 2 + nB) the first rows of the partner segments of its nb antiparallel high bonds (the first
+//   nbr are rung bonds); [2 + nB, 2 + nB + nX) cross bond c: first row of the partner segment;
+//   hop h from word hop_off[h]: nb = 0 or absent: the target's high-part rank; nb 1 or 2: ua, then
+//   the 2^nb high-part ranks by vbi; nb = 3: pi(H << P).
+struct alignas(16) SegDesc {
+    int64_t start;              // the block's first row
+    int64_t rec;                // first word of the block's segment records
+    uint32_t fA[kSegMaxA];      // bonds below P as two-bit flip masks, rung bonds first
+    uint8_t bB[kSegMaxB][2];    // bonds at or above P (a < b): rung, then leg at distance one, then two
+    uint8_t cX[kSegMaxX][2];    // bonds across P: (end below P, end at or above P), rung bonds first
+    uint32_t mr, ma, m2;        // lower ends of the rung / leg-1 / leg-2 bonds at or above P
+    uint8_t nA, nAr, nB, nBr, nBa, nX, nXr, nhop;
+    uint8_t ok, pad[3];         // ok: every term fits the limits above
+    uint32_t rec_len;           // words per segment record, a multiple of 4
+    uint8_t hop_off[kMaxHops];  // first word of hop h in a record
+    uint8_t pad2[4];
+    SegHopDesc hop[kMaxHops];
+};
+static_assert(sizeof(SegDesc) % 16 == 0, "SegDesc is staged as 16-byte words");
+
 // Read-only view of a built sector, passed to kernels by value.
 struct SectorView {
     int L, N, Nh, Nd, Ns;
@@ -133,6 +182,13 @@ struct SectorView {
     int rank_words;                // words of rank_tab
     const uint32_t* comb;          // [33][33] comb[k*33+n] = C(n,k)
     const BlockDesc* desc;         // [n_blocks] fast-row descriptors (null: the orbit-walk row only)
+    // segment layout of free blocks (ed_seg.cuh)
+    int seg_p;                     // P = min(kSegA, Ns)
+    uint32_t seg_off[kSegA + 2];   // first segment of class kl (kl low down spins), kl = 0 .. P + 1
+    const uint32_t* seg_h;         // per segment: its high part H (bits [P, Ns) of dc, shifted down by P)
+    const uint32_t* seg_base;      // per segment: its first row in a block, rank((H << P) | (2^kl - 1))
+    const SegDesc* seg;            // [n_blocks] segment descriptors (free blocks)
+    const uint32_t* seg_rec;       // segment records of every free block (SegDesc::rec, rec_len)
 };
 
 // ---------------------------------------------------------------- bit helpers

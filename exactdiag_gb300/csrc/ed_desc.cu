@@ -13,6 +13,7 @@
 //   * the block's own stabiliser (for resolving exchange targets of non-free blocks).
 // A hop or block whose canonical mask has more than kMaxCand such elements (e.g. the undoped
 // sector) keeps the reference-faithful orbit walk.
+#include <algorithm>
 #include <vector>
 
 #include "ed_internal.cuh"
@@ -81,7 +82,219 @@ int coset(const HostSector& S, uint32_t h, uint32_t hc, CandParams* out) {
     return n;
 }
 
+// Host copy of the hop permutation (ed_seg.cuh: seg_perm).
+uint32_t host_perm(const SegHopDesc& G, uint32_t x, uint32_t nsmask) {
+    const uint32_t xm = (x & G.keep) | (((x & G.band) << G.sl) >> G.sr) | (((x >> G.p) & 1u) << G.q);
+    const uint32_t t = (xm ^ (xm >> 1)) & G.swap;
+    const uint32_t sw = xm ^ t ^ (t << 1);
+    return ((sw << G.rot) | (sw >> G.nsr)) & nsmask;
+}
+
+// Segment descriptor of a free block from its row descriptor: the exchange bonds sorted by where
+// their ends lie relative to P, each hop as a compressed-mask permutation with its target, and the
+// layout of the block's segment records.  copy_index[b]: index of block b's expanded copy among the
+// sector's copies (-1: none).
+SegDesc make_seg_desc(const BlockDesc& D, int Ns, int P, const std::vector<int>& copy_index) {
+    SegDesc G{};
+    G.start = D.start;
+    G.ok = 1;
+    const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
+    const uint32_t amask = (1u << P) - 1u;
+    struct Bond {
+        int a, b, kind;  // kind 0 rung, 1 leg at distance one, 2 leg at distance two, 3 leg across the boundary
+    };
+    std::vector<Bond> bonds;
+    for (uint32_t m = D.m_rung; m; m &= m - 1u) bonds.push_back({ctz32(m), ctz32(m) + 1, 0});
+    for (uint32_t m = D.m_legadj; m; m &= m - 1u) bonds.push_back({ctz32(m), ctz32(m) + 1, 1});
+    for (uint32_t m = D.m_legd2; m; m &= m - 1u) bonds.push_back({ctz32(m), ctz32(m) + 2, 2});
+    for (int u = 0; u < D.nwrap; ++u) bonds.push_back({D.wrap[u][0], D.wrap[u][1], 3});
+    // low and cross bonds: rung bonds first
+    for (int pass = 0; pass < 2; ++pass)
+        for (const Bond& bd : bonds) {
+            if ((bd.kind == 0) != (pass == 0)) continue;
+            const bool rung = bd.kind == 0;
+            if (bd.b < P) {
+                if (G.nA >= kSegMaxA) {
+                    G.ok = 0;
+                    continue;
+                }
+                G.fA[G.nA++] = (1u << bd.a) | (1u << bd.b);
+                if (rung) ++G.nAr;
+            } else if (bd.a >= P) {
+                // high bonds are ranked by kind (rung, leg-1, leg-2) in the kernel: no boundary bonds here
+                if (bd.kind == 3) G.ok = 0;
+            } else {
+                if (G.nX >= kSegMaxX) {
+                    G.ok = 0;
+                    continue;
+                }
+                G.cX[G.nX][0] = (uint8_t)bd.a;
+                G.cX[G.nX][1] = (uint8_t)bd.b;
+                ++G.nX;
+                if (rung) ++G.nXr;
+            }
+        }
+    for (int kind = 0; kind < 3; ++kind)
+        for (const Bond& bd : bonds) {
+            if (bd.kind != kind || bd.a < P) continue;
+            if (G.nB >= kSegMaxB) {
+                G.ok = 0;
+                continue;
+            }
+            G.bB[G.nB][0] = (uint8_t)bd.a;
+            G.bB[G.nB][1] = (uint8_t)bd.b;
+            ++G.nB;
+            if (kind == 0) {
+                ++G.nBr;
+                G.mr |= 1u << bd.a;
+            }
+            if (kind == 1) {
+                ++G.nBa;
+                G.ma |= 1u << bd.a;
+            }
+            if (kind == 2) G.m2 |= 1u << bd.a;
+        }
+    G.nhop = D.nhop;
+    for (int t = 0; t < D.nhop; ++t) {
+        const HopDesc& H = D.hop[t];
+        SegHopDesc& S = G.hop[t];
+        S.p = H.p;
+        S.q = H.q;
+        S.band = H.band;
+        S.sl = H.q > H.p ? 0 : 1;
+        S.sr = (uint8_t)(1 - S.sl);
+        S.keep = ~(H.band | (1u << H.p));
+        S.swap = H.swap;
+        S.rot = H.rot;
+        S.nsr = (uint8_t)((Ns - H.rot) & 31);
+        S.term = H.term;
+        S.sign = H.sign > 0 ? 1 : 0;  // 1: coefficient -w (the hopping term's -t times a positive fermion sign)
+        S.e = H.e;
+        S.tblock = H.block;
+        if (H.mode == kModeFree) {
+            S.kind = 0;
+            S.tstart = H.start;
+        } else if (H.mode == kModeCand && H.block >= 0 && copy_index[H.block] >= 0) {
+            S.kind = 1;
+            S.tstart = copy_index[H.block];
+        } else {
+            S.kind = 3;  // no target block, or a stabiliser target without representatives
+        }
+        const uint32_t above = host_perm(S, amask, nsmask) & ~amask;
+        const int nb = popc32(above);
+        S.nb = (uint8_t)(nb > 2 ? 3 : nb);
+        if (nb >= 1 && nb <= 2) {
+            S.bpos[0] = (uint8_t)ctz32(above);
+            S.bpos[1] = nb == 2 ? (uint8_t)hibit32(above) : 0;
+        }
+        if (S.kind == 3) S.nb = 0;  // an absent hop keeps one record word (0) and contributes nothing
+    }
+    // record layout: header, high-bond partners, cross partners, then each hop's words
+    uint32_t w = 2u + G.nB + G.nX;
+    for (int t = 0; t < D.nhop; ++t) {
+        G.hop_off[t] = (uint8_t)w;
+        const int nb = G.hop[t].nb;
+        w += (nb == 1 || nb == 2) ? 1u + (1u << nb) : 1u;
+    }
+    G.rec_len = (w + 3u) & ~3u;
+    return G;
+}
+
 }  // namespace
+
+// Per class kl = 0 .. P of down spins below P: the high parts H (Ns - P bits, Nd - kl set) in colex
+// order and each segment's first row in a block, the colex rank of (H << P) | (2^kl - 1); off[kl] is
+// the first segment of class kl (off[P + 1] = all segments).
+void seg_tables(int Ns, int Nd, int P, const uint32_t (&comb)[kCombStride][kCombStride], uint32_t* off,
+                std::vector<uint32_t>& hs, std::vector<uint32_t>& bases) {
+    const int B = Ns - P;
+    hs.clear();
+    bases.clear();
+    for (int kl = 0; kl <= P + 1; ++kl) {
+        off[kl] = (uint32_t)hs.size();
+        if (kl > P) break;
+        const int kh = Nd - kl;  // down spins of the high part
+        if (kh < 0 || kh > B) continue;
+        const uint64_t count = comb[kh][B];
+        uint32_t H = kh == 0 ? 0u : ((1u << kh) - 1u);
+        for (uint64_t g = 0; g < count; ++g) {
+            uint32_t r = 0;
+            int j = kl;
+            for (uint32_t m = H; m; m &= m - 1u) {
+                ++j;
+                r += comb[j][P + ctz32(m)];
+            }
+            hs.push_back(H);
+            bases.push_back(r);
+            if (g + 1 < count) H = next_combination(H);
+        }
+    }
+}
+
+// The sector's expanded copies (Sector::copy_blocks) and the segment layout of its free blocks: the
+// segment tables, the segment descriptors and the segment records.
+int build_segments(Sector& s, const std::vector<BlockDesc>& desc, const uint32_t (&comb)[kCombStride][kCombStride]) {
+    SectorView& V = s.view;
+    V.seg = nullptr;
+    V.seg_h = V.seg_base = V.seg_rec = nullptr;
+    const int Ns = V.Ns, Nd = V.Nd;
+    const int P = std::min(kSegA, Ns);
+    V.seg_p = P;
+    // blocks whose values are expanded every step (ExpandTask), in block order: the stabiliser blocks
+    // with rows, and the blocks with a stabiliser that hops out of free blocks reach (whatever kernel
+    // their own rows take); copy_index[b] is b's place in that list
+    std::vector<int> copy_index(V.n_blocks, -1);
+    {
+        std::vector<char> need(V.n_blocks, 0);
+        for (const BlockSpan& sp : s.spans) {
+            if (sp.count <= 0) continue;
+            if (sp.kind == kRowsCand) need[sp.block] = 1;
+            if (sp.kind != kRowsFree) continue;
+            const BlockDesc& D = desc[sp.block];
+            for (int t = 0; t < D.nhop; ++t)
+                if (D.hop[t].mode == kModeCand && D.hop[t].block >= 0 && s.spans[D.hop[t].block].count > 0)
+                    need[D.hop[t].block] = 1;
+        }
+        s.copy_blocks.clear();
+        for (int b = 0; b < V.n_blocks; ++b)
+            if (need[b]) {
+                copy_index[b] = (int)s.copy_blocks.size();
+                s.copy_blocks.push_back(b);
+            }
+    }
+    bool any = false;
+    for (const BlockSpan& sp : s.spans) any = any || sp.kind == kRowsFree;
+    if (!any) return ED_OK;
+    std::vector<uint32_t> hs, bases;
+    seg_tables(Ns, Nd, P, comb, V.seg_off, hs, bases);
+    std::vector<SegDesc> seg(V.n_blocks);
+    std::vector<int> free_blocks;
+    int64_t rec_words = 0;
+    const int64_t nseg = (int64_t)hs.size();
+    for (const BlockSpan& sp : s.spans) {
+        if (sp.kind != kRowsFree) continue;
+        SegDesc& G = seg[sp.block];
+        G = make_seg_desc(desc[sp.block], Ns, P, copy_index);
+        if (!G.ok) return set_error(ED_ERR_INTERNAL, "segments: a free block's terms exceed the segment limits");
+        G.rec = rec_words;
+        rec_words += nseg * (int64_t)G.rec_len;
+        free_blocks.push_back(sp.block);
+    }
+    if (!s.d_seg_h.alloc((int64_t)hs.size()) || !s.d_seg_base.alloc((int64_t)bases.size()) ||
+        !s.d_seg.alloc(V.n_blocks) || !s.d_seg_rec.alloc(rec_words))
+        return set_error(ED_ERR_NOMEM, "segments: device allocation");
+    if (cudaMemcpy(s.d_seg_h.p, hs.data(), hs.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s.d_seg_base.p, bases.data(), bases.size() * sizeof(uint32_t), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(s.d_seg.p, seg.data(), seg.size() * sizeof(SegDesc), cudaMemcpyHostToDevice) != cudaSuccess)
+        return set_error(ED_ERR_CUDA, "segments: upload");
+    V.seg_h = s.d_seg_h.p;
+    V.seg_base = s.d_seg_base.p;
+    V.seg = s.d_seg.p;
+    V.seg_rec = s.d_seg_rec.p;
+    s.host_seg_off.assign(V.seg_off, V.seg_off + P + 2);
+    return seg_records_build(s, free_blocks, nseg);
+}
 
 int build_descriptors(Sector& s) {
     SectorView& V = s.view;
@@ -197,7 +410,7 @@ int build_descriptors(Sector& s) {
     if (cudaMemcpy(s.d_desc.p, desc.data(), desc.size() * sizeof(BlockDesc), cudaMemcpyHostToDevice) != cudaSuccess)
         return set_error(ED_ERR_CUDA, "descriptors: upload");
     V.desc = s.d_desc.p;
-    return ED_OK;
+    return build_segments(s, desc, comb);
 }
 
 }  // namespace ed

@@ -68,6 +68,11 @@ constexpr int kReduceSlots = 4;  // FP64 partial sums per chunk in the fused Lan
 // CTAs running at one time cover a narrow window of rows (the gathered x_j of neighbouring rows
 // stay in L2), large enough to amortise the per-chunk reduction and descriptor staging.
 constexpr int kChunkRows = 8192;
+// The segment kernel of free blocks (ed_seg.cuh): threads per CTA, segments a CTA works on at once at
+// most, and about how many rows one H.v chunk of it holds.
+constexpr int kSegThreads = 256;
+constexpr int kSegSlots = 8;
+constexpr int kSegChunkRows = 16384;
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
 enum RowKind : int {
@@ -86,8 +91,11 @@ struct BlockSpan {
 struct BatchChunk {
     int32_t sec;
     int32_t block;       // descriptor of the chunk's block (every row of a chunk is in one block), or -1
-    int64_t begin, end;  // rows of sector `sec`
-    int64_t xoff;        // stabiliser blocks: first element of the block's expanded copy (ExpandTask), else -1
+    int64_t begin, end;  // rows of sector `sec`; segment chunks: segments [begin, end) of class kl
+    int64_t xoff;        // stabiliser blocks: first element of the block's expanded copy (ExpandTask);
+                         // segment chunks: first element of the sector's copies; else -1
+    int32_t kl;          // segment chunks (free blocks, ed_seg.cuh): down spins below P; row chunks: -1
+    int32_t pad;
 };
 
 // One stabiliser block of a step layout whose vector entries are expanded, every step, to all
@@ -100,15 +108,19 @@ struct ExpandTask {
     int64_t out_off;  // first element of the block's copy in the step layout's expansion scratch
 };
 
-// Chunk tables of a step layout (one sector, or a batch of sectors): all chunks sector-major in
-// row order (the partial sums are indexed by chunk), and the chunk ids grouped by row kind.
+// Chunk tables of a step layout (one sector, or a batch of sectors).  Row chunks cut every sector's
+// rows in order (the update, normalisation and exact-norm passes); H.v chunks are the segment
+// chunks of free blocks and the row chunks of the other blocks, sector-major (the step's partial
+// sums are indexed by H.v chunk), with their ids grouped by row kind.
 struct ChunkPlan {
-    std::vector<BatchChunk> chunks;
-    std::vector<int> kind_idx;
+    std::vector<BatchChunk> chunks;   // row chunks
+    std::vector<int> cfirst, ccount;  // per sector, into chunks
+    std::vector<BatchChunk> hv;       // H.v chunks
+    std::vector<int> hv_first, hv_count;  // per sector, into hv
+    std::vector<int> kind_idx;        // hv ids by kind
     int kind_first[4] = {0, 0, 0, 0};
     int kind_count[4] = {0, 0, 0, 0};
-    std::vector<int> cfirst, ccount;  // per sector
-    std::vector<ExpandTask> tasks;    // stabiliser blocks, in chunk order
+    std::vector<ExpandTask> tasks;    // expanded copies (Sector::copy_blocks of every sector, in order)
     int64_t n_full = 0;               // elements of the expansion scratch
 };
 
@@ -153,6 +165,15 @@ struct Sector {
     int64_t n_full = 0;
     DevBuf<ExpandTask> d_tasks;
     DevBuf<uint8_t> d_xfull;
+    std::vector<int> copy_blocks;  // blocks with an expanded copy, in block order (build_segments)
+    // segment layout of free blocks (build_segments)
+    DevBuf<SegDesc> d_seg;
+    DevBuf<uint32_t> d_seg_h, d_seg_base, d_seg_rec;
+    std::vector<uint32_t> host_seg_off;  // seg_off of the view, kl = 0 .. P + 1
+    // H.v chunks of single-sector steps (ChunkPlan::hv)
+    int n_hv_chunks = 0;
+    DevBuf<BatchChunk> d_hv_chunks;
+    DevBuf<int> d_hv_first, d_hv_count;
 };
 
 // Colex spin-rank tables of Ns spins with Nd down (layout: RankTab): fills V's rk_* fields and
@@ -216,6 +237,7 @@ int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, doub
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
 int single_setup(Sector& s);
 int build_descriptors(Sector& s);
+int seg_records_build(Sector& s, const std::vector<int>& free_blocks, int64_t nseg);  // ed_segrec.cu
 int set_launch(Sector& s, int minb, int ctas_per_sm);
 void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& plan);
 

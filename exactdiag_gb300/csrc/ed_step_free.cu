@@ -1,15 +1,56 @@
 // ed_step_free.cu -- fused step kernel for rows of blocks with a trivial stabiliser (the bulk of
-// every doped sector), in two register budgets: 3 or 4 resident CTAs per SM.
-#include "ed_step.cuh"
+// every doped sector): the segment kernel of ed_seg.cuh, in three register budgets (2, 3 or 4
+// resident CTAs per SM).
+#include "ed_seg.cuh"
 
 namespace ed {
 
-int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st) {
-    return minb == 4 ? step_kind_dtype<4, kRowsFree>(dtype, a, st) : step_kind_dtype<3, kRowsFree>(dtype, a, st);
+namespace {
+
+template <typename R, bool CPLX, int MINB>
+int launch_seg(const StepArgs& a, cudaStream_t st) {
+    if (a.count <= 0) return ED_OK;
+    auto* kern = seg_step_kernel<R, CPLX, MINB>;
+    const int grid = a.grid < a.count ? a.grid : a.count;
+    kern<<<grid, kSegThreads, 0, st>>>(a.views, a.offs, a.chunks, a.idx, a.count, a.w, a.v, a.vprev, a.other, a.first,
+                                       a.scal, a.stride, a.k, a.partials, a.xfull);
+    ED_CHECK_LAUNCH("seg_step_kernel");
+    return ED_OK;
 }
 
-int step_free_occupancy(int minb, size_t smem) {
-    return minb == 4 ? step_kind_occupancy<4, kRowsFree>(smem) : step_kind_occupancy<3, kRowsFree>(smem);
+template <int MINB>
+int seg_dtype(int dtype, const StepArgs& a, cudaStream_t st) {
+    switch (dtype) {
+    case ED_F64: return launch_seg<double, false, MINB>(a, st);
+    case ED_C128: return launch_seg<double, true, MINB>(a, st);
+    case ED_F32: return launch_seg<float, false, MINB>(a, st);
+    default: return launch_seg<float, true, MINB>(a, st);
+    }
+}
+
+template <int MINB>
+int seg_occupancy() {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, seg_step_kernel<float, false, MINB>, kSegThreads, 0) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return per_sm > 0 ? per_sm : 1;
+}
+
+}  // namespace
+
+int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st) {
+    if (minb == 2) return seg_dtype<2>(dtype, a, st);
+    if (minb == 4) return seg_dtype<4>(dtype, a, st);
+    return seg_dtype<3>(dtype, a, st);
+}
+
+int step_free_occupancy(int minb, size_t /*smem*/) {
+    if (minb == 2) return seg_occupancy<2>();
+    if (minb == 4) return seg_occupancy<4>();
+    return seg_occupancy<3>();
 }
 
 }  // namespace ed

@@ -44,7 +44,14 @@ def test_rank_tables_unrank_and_next_combination(tmp_path):
 
 
 def test_chunk_plan_cuts_each_sector_the_same_alone_and_batched(tmp_path):
-    """plan_chunks on synthetic sectors: chunks tile the rows inside their blocks with the per-kind
-    lengths, a sector is cut identically alone and in a batch, stabiliser chunks point at their
-    block's expanded copy."""
+    """plan_chunks on synthetic sectors: row chunks tile the rows inside their blocks with the
+    per-kind lengths, segment chunks tile every class of every free block, a sector is cut
+    identically alone and in a batch, stabiliser chunks point at their block's expanded copy."""
     _build_and_run(tmp_path, "chunk_plan_check")
+
+
+def test_segment_layout_reaches_every_target_rank(tmp_path):
+    """The segment kernel's index arithmetic (ed_seg.cuh helpers, seg_tables) against the colex rank:
+    segments tile each block, and every exchange pair and hop permutation reaches the rank of the
+    flipped or permuted configuration, for Ns = 3 .. 31."""
+    _build_and_run(tmp_path, "seg_layout_check")

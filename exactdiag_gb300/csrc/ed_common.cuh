@@ -114,7 +114,7 @@ static_assert(offsetof(BlockDesc, mode) == 16 && offsetof(BlockDesc, start) == 2
 // low part (bits [0, P)) and a high part H (bits [P, Ns)); the rows sharing H are contiguous (a
 // segment).  SegDesc lists a free block's terms by where their bits lie relative to P.
 
-constexpr int kSegA = 9;      // low compressed bits resolved per thread: C(9, k) <= 126 rows per segment
+constexpr int kSegA = 10;     // low compressed bits resolved per lane: C(10, k) <= 252 rows per segment
 constexpr int kSegMaxA = 16;  // exchange bonds with both ends below P
 constexpr int kSegMaxB = 48;  // exchange bonds with both ends at or above P
 constexpr int kSegMaxX = 8;   // exchange bonds across P
@@ -136,11 +136,13 @@ struct SegHopDesc {
 
 // Per segment of a free block, a record of rec_len 32-bit words (built once per sector by
 // seg_records_kernel; the values depend on the segment's high part only, never on a vector):
-//   [0] the segment's first row in the block;  [1] nb | nbr << 8 | hib << 16;
-//   [2, 2 + nB) the first rows of the partner segments of its nb antiparallel high bonds (the first
-//   nbr are rung bonds); [2 + nB, 2 + nB + nX) cross bond c: first row of the partner segment;
-//   hop h from word hop_off[h]: nb = 0 or absent: the target's high-part rank; nb 1 or 2: ua, then
-//   the 2^nb high-part ranks by vbi; nb = 3: pi(H << P).
+//   [0] the segment's first row in the block;  [1] zbr | zbl << 8 | hib << 16;
+//   [2, 2 + RB) the first rows of the partner segments of its zbr antiparallel high rung bonds, then
+//   the segment's own first row up to a multiple of four; [2 + RB, 2 + RB + LB) the same for its zbl
+//   leg bonds; [xo, xo + nX) cross bond c: first row of the partner segment; hop h from word
+//   hop_off[h]: the first n0 hops (nb = 0, and absent hops) the target's high-part rank; the next n12
+//   (nb 1 or 2) ua, then the 2^nb high-part ranks by vbi; the rest (nb = 3) pi(H << P); then two zero
+//   words (zero_w), which the kernel's padding hops read.
 struct alignas(16) SegDesc {
     int64_t start;              // the block's first row
     int64_t rec;                // first word of the block's segment records
@@ -149,10 +151,10 @@ struct alignas(16) SegDesc {
     uint8_t cX[kSegMaxX][2];    // bonds across P: (end below P, end at or above P), rung bonds first
     uint32_t mr, ma, m2;        // lower ends of the rung / leg-1 / leg-2 bonds at or above P
     uint8_t nA, nAr, nB, nBr, nBa, nX, nXr, nhop;
-    uint8_t ok, pad[3];         // ok: every term fits the limits above
+    uint8_t ok, RB, LB, xo;     // ok: every term fits the limits; record layout (above)
     uint32_t rec_len;           // words per segment record, a multiple of 4
     uint8_t hop_off[kMaxHops];  // first word of hop h in a record
-    uint8_t pad2[4];
+    uint8_t n0, n12, zero_w, pad2;  // hops by kind (record layout above); two zero words from zero_w
     SegHopDesc hop[kMaxHops];
 };
 static_assert(sizeof(SegDesc) % 16 == 0, "SegDesc is staged as 16-byte words");

@@ -187,16 +187,39 @@ SegDesc make_seg_desc(const BlockDesc& D, int Ns, int P, const std::vector<int>&
             S.bpos[0] = (uint8_t)ctz32(above);
             S.bpos[1] = nb == 2 ? (uint8_t)hibit32(above) : 0;
         }
-        if (S.kind == 3) S.nb = 0;  // an absent hop keeps one record word (0) and contributes nothing
+        if (S.kind == 3) S.nb = 0;  // an absent hop keeps one zero record word and contributes nothing
     }
-    // record layout: header, high-bond partners, cross partners, then each hop's words
-    uint32_t w = 2u + G.nB + G.nX;
+    // hops by kind: nb = 0 (and absent), nb 1 or 2, nb 3 (stable within a kind)
+    {
+        SegHopDesc sorted[kMaxHops];
+        int n = 0;
+        for (int cls = 0; cls < 3; ++cls)
+            for (int t = 0; t < D.nhop; ++t) {
+                const int nb = G.hop[t].nb;
+                if ((cls == 0 && nb == 0) || (cls == 1 && (nb == 1 || nb == 2)) || (cls == 2 && nb == 3)) {
+                    sorted[n++] = G.hop[t];
+                    if (cls == 0) ++G.n0;
+                    if (cls == 1) ++G.n12;
+                }
+            }
+        for (int t = 0; t < D.nhop; ++t) G.hop[t] = sorted[t];
+    }
+    // record layout: header, high-bond partners (rung, leg; each padded to a multiple of four), cross
+    // partners, then each hop's words
+    G.RB = (uint8_t)((G.nBr + 3) & ~3);
+    G.LB = (uint8_t)((G.nB - G.nBr + 3) & ~3);
+    uint32_t w = 2u + G.RB + G.LB;
+    G.xo = (uint8_t)w;
+    w += G.nX;
     for (int t = 0; t < D.nhop; ++t) {
         G.hop_off[t] = (uint8_t)w;
         const int nb = G.hop[t].nb;
-        w += (nb == 1 || nb == 2) ? 1u + (1u << nb) : 1u;
+        w += nb == 0 ? 1u : (nb <= 2 ? 1u + (1u << nb) : 1u);
     }
+    G.zero_w = (uint8_t)w;
+    w += 2u;
     G.rec_len = (w + 3u) & ~3u;
+    if (G.rec_len > 128u) G.ok = 0;  // a record is staged in one 16-byte copy per lane of a warp
     return G;
 }
 

@@ -68,10 +68,9 @@ constexpr int kReduceSlots = 4;  // FP64 partial sums per chunk in the fused Lan
 // CTAs running at one time cover a narrow window of rows (the gathered x_j of neighbouring rows
 // stay in L2), large enough to amortise the per-chunk reduction and descriptor staging.
 constexpr int kChunkRows = 8192;
-// The segment kernel of free blocks (ed_seg.cuh): threads per CTA, segments a CTA works on at once at
-// most, and about how many rows one H.v chunk of it holds.
+// The segment kernel of free blocks (ed_seg.cuh): threads per CTA, and about how many rows one H.v
+// chunk of it holds.
 constexpr int kSegThreads = 256;
-constexpr int kSegSlots = 8;
 constexpr int kSegChunkRows = 16384;
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
@@ -95,7 +94,7 @@ struct BatchChunk {
     int64_t xoff;        // stabiliser blocks: first element of the block's expanded copy (ExpandTask);
                          // segment chunks: first element of the sector's copies; else -1
     int32_t kl;          // segment chunks (free blocks, ed_seg.cuh): down spins below P; row chunks: -1
-    int32_t pad;
+    int32_t piece;       // segment chunks of more than 16 rows per segment: rows [32 piece, 32 piece + 32)
 };
 
 // One stabiliser block of a step layout whose vector entries are expanded, every step, to all

@@ -22,9 +22,13 @@
 //     bits above P) and va per thread; otherwise the full rank of U | V is taken per row.
 //     Stabiliser targets read the expanded copy of the target block (expand_cand_kernel) at the same
 //     rank, with the coset's first phase folded in.
-// A thread owns one offset t of every segment in its slot (segments g = begin + slot, + slots, ...);
-// threads never wait on one another inside a chunk.  Each row issues its gathers in groups (low and
-// high bonds eight at a time, cross bonds all at once, hops six at a time) before it adds them up.
+// A warp takes one 32-row piece of a segment (lane = offset in the segment), or several whole
+// segments of at most 16 rows, and walks the chunk's segments with the CTA's other warps; warps never
+// wait on one another inside a chunk, and every per-segment loop bound is the same for all lanes of a
+// warp.  The per-lane terms of a chunk live in shared memory (every warp maps its lanes to the same
+// offsets).  While a warp works on one segment, the next segment's record is copied into shared
+// memory (cp.async) and its row value loaded, so a row's gathers wait on one round trip per group
+// (low bonds, high bonds four at a time, cross bonds, hops) rather than on chains of dependent loads.
 // The key table is not read: a free row's configuration follows from its index.
 //
 // Per-row sums of the step (ed_step.cuh) are kept per thread in plain FP32 (FP64) over four rows and
@@ -90,18 +94,17 @@ __host__ __device__ __forceinline__ uint32_t seg_hop_base(uint32_t U, uint32_t a
     return spin_rank(mB | ((1u << klt) - 1u), R, Nd);
 }
 
-// Per-thread part of a hop: rank_P(V) when nb = 0, else V's low bits and vbi (bits 9, 10).
+// Per-lane part of a hop (nb <= 2): V's low bits and, above them (bits kSegA, kSegA + 1), vbi.
 __host__ __device__ __forceinline__ uint32_t seg_hop_thread(uint32_t V, uint32_t amask, uint32_t nb, uint32_t bp0,
-                                                            uint32_t bp1, const uint8_t* rt) {
-    if (nb == 0) return rt[V];
-    return (V & amask) | ((((V >> bp0) & 1u) | (nb == 2 ? ((V >> bp1) & 1u) << 1 : 0u)) << 9);
+                                                            uint32_t bp1) {
+    const uint32_t vbi = nb == 0 ? 0u : (((V >> bp0) & 1u) | (nb == 2 ? ((V >> bp1) & 1u) << 1 : 0u));
+    return (V & amask) | (vbi << kSegA);
 }
 
-// Target rank of a hop (nb <= 2) from its per-segment (sb, ua) and per-thread (hc) parts.
-__host__ __device__ __forceinline__ uint32_t seg_hop_rank(uint32_t nb, const uint32_t* sb, uint32_t ua, uint32_t hc,
+// Target rank of a hop (nb <= 2) from its per-segment (ua, sb) and per-lane (hc) parts.
+__host__ __device__ __forceinline__ uint32_t seg_hop_rank(const uint32_t* sb, uint32_t ua, uint32_t hc,
                                                           const uint8_t* rt) {
-    if (nb == 0) return sb[0] + hc;
-    return sb[hc >> 9] + rt[ua | (hc & 511u)];
+    return sb[hc >> kSegA] + rt[ua | (hc & (kSegLow - 1u))];
 }
 
 // A hop of the chunk's block as the rows use it (built per chunk from SegHopDesc and the weights).
@@ -126,6 +129,10 @@ __device__ __forceinline__ void seg_ld(const typename Vec<R, CPLX>::T* p, R& re,
     }
 }
 
+// Fused multiply-add in the vectors' own precision (FP32 stays FP32).
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 template <typename R>
 __device__ __forceinline__ void fold(Accum<R>& a, R p);
 template <>
@@ -137,6 +144,19 @@ __device__ __forceinline__ void fold(Accum<float>& a, float p) {
     a.add(p, 0.0f);
 }
 
+constexpr int kSegRecMax = 128;  // words of a staged segment record (one 16-byte copy per lane)
+constexpr int kSegHopSlots = 24; // hops of a block padded to groups of four per kind (at most 12 + 12)
+
+__device__ __forceinline__ void seg_cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void seg_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void seg_cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 template <typename R, bool CPLX, int MINB>
 __global__ void __launch_bounds__(kSegThreads, MINB)
     seg_step_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
@@ -144,11 +164,26 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     void* v, void* vprev, void* other, int first, const double* __restrict__ scal, int stride, int k,
                     double* __restrict__ partials, void* xfull) {
     using T = typename Vec<R, CPLX>::T;
+    constexpr int kWarps = kSegThreads / 32;
     __shared__ uint8_t s_rt[kSegLow];           // rank_P of each P-bit mask within its popcount class
     __shared__ uint16_t s_ut[kSegLow];          // the masks by (popcount, rank_P)
     __shared__ uint32_t s_utoff[kSegA + 2];
     __shared__ __align__(16) SegDesc s_desc;
     __shared__ __align__(16) SegHop<R, CPLX> s_hop[kMaxHops];
+    // hop slots of the chunk: the kind-0 hops then dummies up to a multiple of four, the same for kind 1
+    // (nb 1 or 2); a dummy reads the first element of the block with coefficient 0
+    __shared__ const T* s_stp[kSegHopSlots];
+    __shared__ R s_scr[kSegHopSlots], s_sci[kSegHopSlots];
+    __shared__ uint32_t s_soff[kSegHopSlots];
+    // per-lane terms of the chunk (every warp maps its lanes to the same offsets t)
+    __shared__ uint8_t s_ar[8][32];             // rank_P of the rung-bond partners below P, padded with t
+    __shared__ uint8_t s_al[16][32];            // the same for leg bonds
+    __shared__ uint8_t s_xo[kSegMaxX][32];      // cross bond c: rank_P(Lo ^ low end) (0 past nX)
+    __shared__ uint16_t s_hc[kSegHopSlots][32]; // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA (kind 1)
+    __shared__ uint32_t s_lane[32];             // Lo | lob << 16 (cross-bond low-end spins)
+    __shared__ uint32_t s_cnt[32];              // nr | nl << 8 (antiparallel low bonds by kind)
+    __shared__ int s_max[2];                    // the chunk's longest rung and leg lists, in fours
+    __shared__ __align__(16) uint32_t s_rec[kWarps][2][kSegRecMax];  // per warp: this and the next record
     const int P = views[0].seg_p;
     const uint32_t amask = (1u << P) - 1u;
     const uint32_t* __restrict__ comb = views[0].comb;
@@ -171,6 +206,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     __syncthreads();
     for (int m = threadIdx.x; m < (1 << P); m += blockDim.x) s_ut[s_utoff[__popc(m)] + s_rt[m]] = (uint16_t)m;
     const R wr = R(0.5) * (R)W.w[3], wl = R(0.5) * (R)W.w[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     for (int c = blockIdx.x; c < count; c += gridDim.x) {
         const int cid = idx[c];
@@ -179,24 +215,24 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int kl = ch.kl, Ns = Sp->Ns, Nd = Sp->Nd, N = Sp->N, L = Sp->L;
         const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
         const int nA = (int)comb[kl * kCombStride + P];
-        const int nslots = min(kSegSlots, (kSegThreads - 1) / nA);
-        const int slot = (int)threadIdx.x / nA, t = (int)threadIdx.x - slot * nA;
-        const bool act = slot < nslots;
-        __syncthreads();  // the previous chunk's rows are done with the shared descriptor and hops
+        const int t = 32 * ch.piece + lane;   // a warp takes one 32-row piece of a segment
+        const int nact = min(32, nA - 32 * ch.piece);
+        const bool act = lane < nact;
+        __syncthreads();  // the previous chunk's rows are done with the shared tables
         {
             const uint4* src = reinterpret_cast<const uint4*>(Sp->seg + ch.block);
             uint4* dst = reinterpret_cast<uint4*>(&s_desc);
             for (int i = threadIdx.x; i < (int)(sizeof(SegDesc) / 16); i += blockDim.x) dst[i] = src[i];
         }
         __syncthreads();
-        const int nhop = s_desc.nhop, nX = s_desc.nX, nXr = s_desc.nXr;
+        const int nhop = s_desc.nhop, n0 = s_desc.n0, n12 = s_desc.n12, nX = s_desc.nX, nXr = s_desc.nXr;
         const int64_t bstart = s_desc.start;
         T* const x = reinterpret_cast<T*>(v) + offs[ch.sec];
         const T* const xb = x + bstart;
-        if ((int)threadIdx.x < kMaxHops) {
+        if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + kMaxHops) {
             // every hop slot gets a record: absent hops (and slots past nhop) read a valid element with
             // coefficient 0
-            const int h = threadIdx.x;
+            const int h = threadIdx.x - 32;
             SegHop<R, CPLX>& F = s_hop[h];
             const SegHopDesc& G = s_desc.hop[h];
             const bool live = h < nhop && G.kind != 3 && W.w[G.term] != 0.0;
@@ -236,104 +272,176 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
             }
         }
-        __syncthreads();
-
-        // ---- per-thread terms of Lo (fixed for every segment of the chunk)
-        uint64_t aw0 = 0, aw1 = 0;   // rank_P of the antiparallel low-bond partners (bytes; 0 past na)
-        uint64_t xw = 0;             // cross bond c: rank_P(Lo ^ low end) (byte c)
-        uint32_t hw[kMaxHops / 2] = {0, 0, 0, 0, 0, 0};  // hop: 16-bit rank_P(V) (nb 0) or va | vbi << 9
-        uint32_t lo = 0, lob = 0;
-        int na = 0, nar = 0;
-        if (act) {
-            lo = s_ut[s_utoff[kl] + t];
+        if (warp == 0) {
+            // the per-lane tables; the partner lists are padded with the row's own offset to their full
+            // length (the padding is read in groups of four and taken back out after the sums)
+            const uint32_t lo = act ? s_ut[s_utoff[kl] + t] : 0u;
+            const uint8_t tt = (uint8_t)(act ? t : 0);
+            int nr = 0, nl = 0;
             const int nAb = s_desc.nA, nAr = s_desc.nAr;
-            for (int i = 0; i < nAb; ++i) {
+            for (int i = 0; i < nAb && act; ++i) {
                 const uint32_t f = s_desc.fA[i], sb = lo & f;
                 if (sb != 0u && sb != f) {
-                    const uint64_t o = (uint64_t)s_rt[lo ^ f];
-                    if (na < 8) aw0 |= o << (8 * na);
-                    else aw1 |= o << (8 * (na - 8));
-                    ++na;
-                    if (i < nAr) ++nar;
+                    if (i < nAr) s_ar[nr++][lane] = s_rt[lo ^ f];
+                    else s_al[nl++][lane] = s_rt[lo ^ f];
                 }
             }
-#pragma unroll
+            const int mr = (int)__reduce_max_sync(0xffffffffu, (unsigned)nr);
+            const int ml = (int)__reduce_max_sync(0xffffffffu, (unsigned)nl);
+            for (int q = nr; q < 8; ++q) s_ar[q][lane] = tt;
+            for (int q = nl; q < 16; ++q) s_al[q][lane] = tt;
+            uint32_t lob = 0;
             for (int cc = 0; cc < kSegMaxX; ++cc) {
-                if (cc < nX) {
-                    const uint32_t a = s_desc.cX[cc][0];
-                    lob |= ((lo >> a) & 1u) << cc;
-                    xw |= (uint64_t)s_rt[lo ^ (1u << a)] << (8 * cc);
-                }
+                const uint32_t a = s_desc.cX[cc][0];
+                if (cc < nX) lob |= ((lo >> a) & 1u) << cc;
+                s_xo[cc][lane] = act && cc < nX ? s_rt[lo ^ (1u << a)] : (uint8_t)0;
             }
-#pragma unroll
-            for (int h = 0; h < kMaxHops; ++h) {
-                const SegHop<R, CPLX>& F = s_hop[h];
-                if (h < nhop && F.kind != 3 && F.nb < 3) {
-                    const uint32_t V = seg_perm(lo, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                    hw[h >> 1] |= seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1, s_rt) << (16 * (h & 1));
-                }
+            s_lane[lane] = lo | (lob << 16);
+            s_cnt[lane] = (uint32_t)nr | ((uint32_t)nl << 8);
+            if (lane == 0) {
+                s_max[0] = (mr + 3) & ~3;
+                s_max[1] = (ml + 3) & ~3;
             }
         }
-        const int namax = (int)__reduce_max_sync(0xffffffffu, (unsigned)na);
-        bool ngen = false;  // the block has hops that take the full rank per row
-        for (int h = 0; h < nhop; ++h) ngen = ngen || (s_hop[h].nb >= 3 && s_hop[h].kind != 3);
-        const uint32_t rec_len = s_desc.rec_len;
+        __syncthreads();
+        const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
+        if (warp == 0) {
+            const uint32_t lo = s_lane[lane] & 0xffffu;
+            for (int sl = 0; sl < n04 + n124; ++sl) {
+                const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
+                uint32_t hc = 0;
+                if (act && h >= 0 && s_hop[h].kind != 3) {
+                    const SegHop<R, CPLX>& F = s_hop[h];
+                    const uint32_t V = seg_perm(lo, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
+                    hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
+                }
+                s_hc[sl][lane] = (uint16_t)hc;
+            }
+        } else if (warp == 1 && lane < n04 + n124) {
+            const int sl = lane;
+            const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
+            s_stp[sl] = h >= 0 ? s_hop[h].tp : xb;
+            s_scr[sl] = h >= 0 ? s_hop[h].cr : R(0);
+            s_sci[sl] = h >= 0 ? s_hop[h].ci : R(0);
+            s_soff[sl] = h >= 0 ? s_desc.hop_off[h] : s_desc.zero_w;
+        }
+        __syncthreads();
+
+        const int mr4 = s_max[0], ml4 = s_max[1];  // list lengths read, rounded up to groups of four
+        const uint32_t cnt = s_cnt[lane], ln = s_lane[lane];
+        const int nr = (int)(cnt & 255u), nl = (int)(cnt >> 8);
+        const uint32_t lo = ln & 0xffffu, lob = ln >> 16;
+        const int pad_r = mr4 - nr, pad_l = ml4 - nl;
+        const uint32_t rec_len = s_desc.rec_len, RB = s_desc.RB, xo = s_desc.xo;
         const uint32_t* __restrict__ rec0 = Sp->seg_rec + s_desc.rec + (int64_t)Sp->seg_off[kl] * rec_len;
-        const uint32_t xoff_w = 2u + s_desc.nB;  // first cross-partner word
+        const uint32_t* __restrict__ segb = Sp->seg_base + Sp->seg_off[kl];
+        const int nX4 = (nX + 3) & ~3;  // cross bonds read in groups of four (the padding is never antiparallel)
+        const uint32_t xall = (1u << nX) - 1u, xrmask = (1u << nXr) - 1u, xlmask = ((1u << nX4) - 1u) & ~xrmask;
         T* const y = reinterpret_cast<T*>(other) + offs[ch.sec] + bstart;
         const T* const yp = first ? nullptr : reinterpret_cast<const T*>(vprev) + offs[ch.sec] + bstart;
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
+        const T* const xt = xb + t;  // this row's offset in every segment of the block
+        uint32_t* const srec0 = s_rec[warp][0];
+        uint32_t* const srec1 = s_rec[warp][1];
 
         Accum<R> acc[kReduceSlots];
         R pend[kReduceSlots] = {R(0), R(0), R(0), R(0)};
         int npend = 0;
-        for (int64_t g = ch.begin + slot; act && g < ch.end; g += nslots) {
-            const uint32_t* __restrict__ rec = rec0 + g * (int64_t)rec_len;
-            const uint32_t base = __ldg(rec), w1 = __ldg(rec + 1);
-            const int zb = (int)(w1 & 255u), zbr = (int)((w1 >> 8) & 255u);
-            const uint32_t hib = w1 >> 16;
+
+        // the next segment's record is copied into shared memory, and its row value and v_{k-1} loaded,
+        // while this one is worked on; the piece's active lanes together copy every word of a record
+        int64_t g = act ? ch.begin + warp : ch.end;  // lanes past the piece's rows skip to the reduction
+        if (g < ch.end)
+            for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
+                seg_cp_async16(srec0 + w4, rec0 + g * (int64_t)rec_len + w4);
+        seg_cp_commit();
+        uint32_t base = 0;
+        R xr = R(0), xi = R(0), pr = R(0), pi = R(0);
+        if (g < ch.end) {
+            base = __ldg(segb + g);
+            seg_ld<R, CPLX>(xt + base, xr, xi);
+            if (!first) seg_ld<R, CPLX>(yp + base + t, pr, pi);
+        }
+        for (int it = 0; g < ch.end; ++it, g += kWarps) {
+            const uint32_t* const sw = (it & 1) ? srec1 : srec0;
+            const int64_t gn = g + kWarps;
+            if (gn < ch.end) {
+                uint32_t* const dst = (it & 1) ? srec0 : srec1;
+                for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
+                    seg_cp_async16(dst + w4, rec0 + gn * (int64_t)rec_len + w4);
+            }
+            seg_cp_commit();
+            uint32_t nbase = 0;
+            R nxr = R(0), nxi = R(0), npr = R(0), npi = R(0);
+            if (gn < ch.end) {
+                nbase = __ldg(segb + gn);
+                seg_ld<R, CPLX>(xt + nbase, nxr, nxi);
+                if (!first) seg_ld<R, CPLX>(yp + nbase + t, npr, npi);
+            }
+            seg_cp_wait<1>();  // this segment's record has arrived (the next one may be in flight)
+            __syncwarp(__activemask());
+
+            // ---- the row: y = H x - beta v_{k-1} at offset t of segment g
+            const uint32_t w1 = sw[1];
+            const int zbr = (int)(w1 & 255u), zbl = (int)((w1 >> 8) & 255u);
+            const int zbr4 = (zbr + 3) & ~3, zbl4 = (zbl + 3) & ~3;
+            const uint32_t xm = (lob ^ (w1 >> 16)) & xall;
             const T* const xs = xb + base;  // the segment
-            const T* const xt = xb + t;     // this row's offset in every segment of the block
-            R xr, xi, pr = R(0), pi = R(0);
-            seg_ld<R, CPLX>(xs + t, xr, xi);
-            if (!first) seg_ld<R, CPLX>(yp + base + t, pr, pi);  // v_{k-1}; may share y's buffer (read first)
             R arr = R(0), ari = R(0), alr = R(0), ali = R(0), hr = R(0), hi = R(0);
-            // exchange bonds below P: partners in the same segment (L1), eight loads in flight
+            // exchange bonds below P: partners in the same segment, four loads at a time
+            for (int q0 = 0; q0 < mr4; q0 += 4) {
+                R vr[4], vi[4];
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                if (half * 8 < namax) {
-                    const uint64_t aw = half ? aw1 : aw0;
-                    R vr[8], vi[8];
+                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xs + s_ar[q0 + u][lane], vr[u], vi[u]);
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) seg_ld<R, CPLX>(xs + (uint32_t)((aw >> (8 * u)) & 255u), vr[u], vi[u]);
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int q = half * 8 + u;
-                        if (q >= na) continue;
-                        if (q < nar) {
-                            arr += vr[u];
-                            if constexpr (CPLX) ari += vi[u];
-                        } else {
-                            alr += vr[u];
-                            if constexpr (CPLX) ali += vi[u];
-                        }
-                    }
+                for (int u = 0; u < 4; ++u) {
+                    arr += vr[u];
+                    if constexpr (CPLX) ari += vi[u];
                 }
             }
-            // exchange bonds at or above P: the partner segments at the same offset, eight loads in flight
-            for (int q0 = 0; q0 < zb; q0 += 8) {
-                R vr[8], vi[8];
+            for (int q0 = 0; q0 < ml4; q0 += 4) {
+                R vr[4], vi[4];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int q = q0 + u;
-                    const uint32_t o = q < zb ? __ldg(rec + 2 + q) : 0u;
-                    seg_ld<R, CPLX>(xt + o, vr[u], vi[u]);
+                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xs + s_al[q0 + u][lane], vr[u], vi[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    alr += vr[u];
+                    if constexpr (CPLX) ali += vi[u];
+                }
+            }
+            // exchange bonds at or above P: the partner segments at the same offset, four at a time
+            for (int q0 = 0; q0 < zbr4; q0 += 4) {
+                R vr[4], vi[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xt + sw[2 + q0 + u], vr[u], vi[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    arr += vr[u];
+                    if constexpr (CPLX) ari += vi[u];
+                }
+            }
+            for (int q0 = 0; q0 < zbl4; q0 += 4) {
+                R vr[4], vi[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xt + sw[2 + RB + q0 + u], vr[u], vi[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    alr += vr[u];
+                    if constexpr (CPLX) ali += vi[u];
+                }
+            }
+            // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
+            for (int c0 = 0; c0 < nX4; c0 += 4) {
+                R vr[4], vi[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int cc = c0 + u;
+                    const uint32_t o = ((xm >> cc) & 1u) ? sw[xo + cc] + s_xo[cc][lane] : base + (uint32_t)t;
+                    seg_ld<R, CPLX>(xb + o, vr[u], vi[u]);
                 }
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int q = q0 + u;
-                    if (q >= zb) continue;
-                    if (q < zbr) {
+                for (int u = 0; u < 4; ++u) {
+                    if (c0 + u < nXr) {
                         arr += vr[u];
                         if constexpr (CPLX) ari += vi[u];
                     } else {
@@ -342,72 +450,49 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     }
                 }
             }
-            // bonds across P (antiparallel when the two ends' spins differ)
-            const uint32_t xm = (lob ^ hib) & ((1u << nX) - 1u);
-            {
-                R vr[kSegMaxX], vi[kSegMaxX];
+            // the padding read the row itself: take it back out
+            const R off_r = (R)(pad_r + (zbr4 - zbr) + __popc(~xm & xrmask));
+            const R off_l = (R)(pad_l + (zbl4 - zbl) + __popc(~xm & xlmask));
+            arr -= off_r * xr;
+            alr -= off_l * xr;
+            if constexpr (CPLX) {
+                ari -= off_r * xi;
+                ali -= off_l * xi;
+            }
+            // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
+            for (int h0 = 0; h0 < n04 + n124; h0 += 4) {
+                R vr[4], vi[4];
+                if (h0 < n04) {
 #pragma unroll
-                for (int cc = 0; cc < kSegMaxX; ++cc) {
-                    vr[cc] = vi[cc] = R(0);
-                    if (cc < nX) {
-                        const bool on = (xm >> cc) & 1u;
-                        const uint32_t o = on ? __ldg(rec + xoff_w + cc) + (uint32_t)((xw >> (8 * cc)) & 255u) : 0u;
-                        seg_ld<R, CPLX>(xb + o, vr[cc], vi[cc]);
-                        if (!on) vr[cc] = vi[cc] = R(0);
+                    for (int u = 0; u < 4; ++u)
+                        seg_ld<R, CPLX>(s_stp[h0 + u] + sw[s_soff[h0 + u]] + s_hc[h0 + u][lane], vr[u], vi[u]);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const uint32_t off = s_soff[h0 + u], hc = s_hc[h0 + u][lane];
+                        const uint32_t r = sw[off + 1 + (hc >> kSegA)] + s_rt[sw[off] | (hc & (kSegLow - 1u))];
+                        seg_ld<R, CPLX>(s_stp[h0 + u] + r, vr[u], vi[u]);
                     }
                 }
 #pragma unroll
-                for (int cc = 0; cc < kSegMaxX; ++cc) {
-                    if (cc < nXr) {
-                        arr += vr[cc];
-                        if constexpr (CPLX) ari += vi[cc];
-                    } else {
-                        alr += vr[cc];
-                        if constexpr (CPLX) ali += vi[cc];
+                for (int u = 0; u < 4; ++u) {
+                    const R cr = s_scr[h0 + u];
+                    hr += cr * vr[u];
+                    if constexpr (CPLX) {
+                        const R ci = s_sci[h0 + u];
+                        hr -= ci * vi[u];
+                        hi += cr * vi[u] + ci * vr[u];
                     }
                 }
             }
-            // hops: six target addresses, then their loads, then the products
-#pragma unroll
-            for (int h0 = 0; h0 < kMaxHops; h0 += 6) {
-                if (h0 < nhop) {
-                    R vr[6], vi[6];
-#pragma unroll
-                    for (int u = 0; u < 6; ++u) {
-                        const int h = h0 + u;
-                        vr[u] = vi[u] = R(0);
-                        if (h < nhop && s_hop[h].nb < 3) {
-                            const SegHop<R, CPLX>& F = s_hop[h];
-                            const uint32_t* hr_ = rec + s_desc.hop_off[h];
-                            const uint32_t hc = (hw[h >> 1] >> (16 * (h & 1))) & 0xffffu;
-                            const uint32_t r = F.nb == 0 ? __ldg(hr_) + hc
-                                                         : __ldg(hr_ + 1 + (hc >> 9)) + s_rt[__ldg(hr_) | (hc & 511u)];
-                            seg_ld<R, CPLX>(F.tp + r, vr[u], vi[u]);
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 6; ++u) {
-                        const int h = h0 + u;
-                        if (h < nhop) {
-                            const R cr = s_hop[h].cr, ci = s_hop[h].ci;
-                            hr += cr * vr[u];
-                            if constexpr (CPLX) {
-                                hr -= ci * vi[u];
-                                hi += cr * vi[u] + ci * vr[u];
-                            }
-                        }
-                    }
-                }
-            }
-            if (ngen) {
+            if (n0 + n12 < nhop) {
                 // hops that move more than two low positions above P: the full rank of U | V
                 const RankTab RT = rank_tab_of(*Sp, Sp->rank_tab);
 #pragma unroll 1
-                for (int h = 0; h < nhop; ++h) {
+                for (int h = n0 + n12; h < nhop; ++h) {
                     const SegHop<R, CPLX>& F = s_hop[h];
-                    if (F.nb < 3 || F.kind == 3) continue;
                     const uint32_t V = seg_perm(lo, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                    const uint32_t r = spin_rank(__ldg(rec + s_desc.hop_off[h]) | V, RT, Nd);
+                    const uint32_t r = spin_rank(sw[s_desc.hop_off[h]] | V, RT, Nd);
                     R vr, vi;
                     seg_ld<R, CPLX>(F.tp + r, vr, vi);
                     hr += F.cr * vr;
@@ -418,23 +503,21 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
             }
             // diagonal: -J/2 per antiparallel bond
-            const uint32_t rmask = (1u << nXr) - 1u;
-            const R diag = -(wr * (R)(nar + zbr + __popc(xm & rmask)) +
-                             wl * (R)((na - nar) + (zb - zbr) + __popc(xm & ~rmask)));
+            const R diag = -(wr * (R)(nr + zbr + __popc(xm & xrmask)) + wl * (R)(nl + zbl + __popc(xm & xlmask)));
             const R h_r = wr * arr + wl * alr + hr + diag * xr;
             const R h_i = CPLX ? (wr * ari + wl * ali + hi + diag * xi) : R(0);
             const R yr = h_r - beta * pr;
             const R yi = CPLX ? h_i - beta * pi : R(0);
             st<R, CPLX>(y, (int64_t)base + t, yr, yi);
-            pend[0] = fma(xr, h_r, pend[0]);
-            pend[1] = fma(yr, yr, pend[1]);
-            pend[2] = fma(xr, yr, pend[2]);
-            pend[3] = fma(xr, xr, pend[3]);
+            pend[0] = fma_r(xr, h_r, pend[0]);
+            pend[1] = fma_r(yr, yr, pend[1]);
+            pend[2] = fma_r(xr, yr, pend[2]);
+            pend[3] = fma_r(xr, xr, pend[3]);
             if constexpr (CPLX) {
-                pend[0] = fma(xi, h_i, pend[0]);
-                pend[1] = fma(yi, yi, pend[1]);
-                pend[2] = fma(xi, yi, pend[2]);
-                pend[3] = fma(xi, xi, pend[3]);
+                pend[0] = fma_r(xi, h_i, pend[0]);
+                pend[1] = fma_r(yi, yi, pend[1]);
+                pend[2] = fma_r(xi, yi, pend[2]);
+                pend[3] = fma_r(xi, xi, pend[3]);
             }
             if (++npend == 4) {
 #pragma unroll
@@ -444,7 +527,14 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
                 npend = 0;
             }
+            __syncwarp(__activemask());  // every lane is done with this buffer before it is refilled
+            base = nbase;
+            xr = nxr;
+            xi = nxi;
+            pr = npr;
+            pi = npi;
         }
+        seg_cp_wait<0>();
 #pragma unroll
         for (int q = 0; q < kReduceSlots; ++q) fold<R>(acc[q], pend[q]);
         if constexpr (sizeof(R) == 4) {

@@ -179,8 +179,8 @@ void check_sector(int Ns, int Nd, std::mt19937_64& rng, long hop_counts[4]) {
                 uint32_t sb[4] = {0, 0, 0, 0};
                 for (int vbi = 0; vbi < (1 << G.nb); ++vbi)
                     sb[vbi] = seg_hop_base(U, amask, vbi, G.bpos[0], G.bpos[1], P, R, Nd);
-                const uint32_t hc = seg_hop_thread(Vp, amask, G.nb, G.bpos[0], G.bpos[1], rt);
-                got = seg_hop_rank(G.nb, sb, U & amask, hc, rt);
+                const uint32_t hc = seg_hop_thread(Vp, amask, G.nb, G.bpos[0], G.bpos[1]);
+                got = seg_hop_rank(sb, U & amask, hc, rt);
             }
             ++hop_counts[G.nb];
             expect(got == want, "hop target", Ns, Nd, dc);

@@ -324,6 +324,8 @@ int ed_project_out(ed_sector* h, int dtype, const void* basis_dev, int k, void* 
                    void* stream) {
     if (!h || !basis_dev || !w_dev || k < 0) return set_error(ED_ERR_INVALID, "ed_project_out: bad argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_project_out: basis not built");
+    if ((dtype == ED_F64 || dtype == ED_F32) && !h->s.real)
+        return set_error(ED_ERR_INVALID, "ed_project_out: real dtype with a complex sector");
     if (k == 0) return ED_OK;
     Sector& s = h->s;
     const int64_t need = (int64_t)k * 2 * s.num_sms * kReduceSlots + 2 * (int64_t)k;
@@ -339,6 +341,8 @@ int ed_project_out_noalloc(const ed_sector* h, int dtype, const void* basis_dev,
                            void* stream) {
     if (!h || !basis_dev || !w_dev) return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_project_out_noalloc: basis not built");
+    if ((dtype == ED_F64 || dtype == ED_F32) && !h->s.real)
+        return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: real dtype with a complex sector");
     return project_noalloc_launch(h->s, dtype, basis_dev, k, w_dev, coef_dev, (cudaStream_t)stream);
 }
 

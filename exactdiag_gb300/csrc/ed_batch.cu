@@ -12,7 +12,6 @@
 //
 // Projection (full reorthogonalisation for the lowest-eigenpair solver):
 // w <- w - sum_j <v_j, w> v_j with FP64 dot products.
-#include <mutex>
 #include <vector>
 
 #include "ed_step.cuh"
@@ -840,23 +839,15 @@ constexpr int64_t kNoAllocScratchDoubles =
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
-// Device address of the array for the current device, looked up once per device (host code may
-// not use the symbol itself: on the host it names a stand-in, not device memory).
+// Device address of the array in the current device's context.  Looked up on every call (a cheap
+// host-side query, not a stream operation): a cached address would dangle once a context is torn down
+// and the module reloaded elsewhere (host code may not use the symbol itself: on the host it names a
+// stand-in, not device memory).
 static int noalloc_scratch_address(double** out) {
-    static std::mutex mu;
-    static double* addr[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= 64) return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: device ordinal above 63");
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetSymbolAddress");
-        addr[dev] = static_cast<double*>(p);
-    }
-    *out = addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetSymbolAddress");
+    *out = static_cast<double*>(p);
     return ED_OK;
 }
 
@@ -866,6 +857,11 @@ int project_noalloc_launch(const Sector& s, int dtype, const void* V, int k, voi
     if (k > kNoAllocMaxVectors)
         return set_error(ED_ERR_TOO_LARGE, "ed_project_out_noalloc: k exceeds the fixed scratch (at most 256 vectors)");
     if (k == 0 || s.view.n == 0) return ED_OK;
+    int dev = 0;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e, "ed_project_out_noalloc: cudaGetDevice");
+    if (dev != s.device)
+        return set_error(ED_ERR_INVALID, "ed_project_out_noalloc: the current device is not the sector's device");
     double* scratch = nullptr;
     if (int rc = noalloc_scratch_address(&scratch)) return rc;
     int nchunks = (int)std::min<int64_t>(kNoAllocMaxChunks, (s.view.n + 1023) / 1024);

@@ -436,7 +436,8 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int cc = c0 + u;
-                    const uint32_t o = ((xm >> cc) & 1u) ? sw[xo + cc] + s_xo[cc][lane] : base + (uint32_t)t;
+                    const uint32_t on = 0u - ((xm >> cc) & 1u);  // all ones when antiparallel (no branch)
+                    const uint32_t o = (on & (sw[xo + cc] + s_xo[cc][lane])) | (~on & (base + (uint32_t)t));
                     seg_ld<R, CPLX>(xb + o, vr[u], vi[u]);
                 }
 #pragma unroll

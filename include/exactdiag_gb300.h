@@ -197,14 +197,15 @@ int ed_project_out(ed_sector* s, int dtype, const void* basis_dev, int k, void* 
 
 /* The same projection as ed_project_out, allocating nothing.  No counterpart in the
  * reference.  ed_project_out grows a per-sector scratch buffer with cudaMalloc on its first
- * call with a larger k, which some callers cannot allow: code being captured into a CUDA graph
- * (an allocation and the synchronisation it needs break the capture), and services that run
- * under a fixed device-memory budget or their own allocator.  This variant keeps its scratch
- * (per-chunk partial dot products and the coefficients) in one fixed device array of 2.1 MB
- * that every GPU loading the library holds until the process exits; k is limited to 256
- * vectors (ED_ERR_TOO_LARGE above).  The first call on each device looks up the array's device
- * address; make that first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (other streams or threads) race.  coef_dev as in ed_project_out. */
+ * call with a larger k, which some callers cannot allow: services that run under a fixed
+ * device-memory budget or hand all device memory to their own allocator, and callers that may
+ * not synchronise the device in the middle of their work (cudaMalloc can).  This variant keeps
+ * its scratch (per-chunk partial dot products and the coefficients) in one fixed device array
+ * of 2.1 MB that every GPU loading the library holds until the process exits; k is limited to
+ * 256 vectors (ED_ERR_TOO_LARGE above).  Each call looks up the array's address in the current
+ * device's context (a host-side query) and must be made with the sector's device current
+ * (ED_ERR_INVALID otherwise).  All calls share the array: calls that overlap on the GPU (other
+ * streams or threads) race.  coef_dev as in ed_project_out. */
 int ed_project_out_noalloc(const ed_sector* s, int dtype, const void* basis_dev, int k, void* w_dev, double* coef_dev,
                            void* stream);
 

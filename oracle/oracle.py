@@ -32,7 +32,9 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libedoracle.so"
 REF_PATH = HERE / "_ref" / "libedref.so"
-REF_SRC = pathlib.Path(os.environ.get("EXACTDIAG_REF_SRC", "/root/reference/src/exactdiag"))
+# the reference's src/exactdiag directory, when a checkout is at hand (oracle/_ref and the tests that
+# compare with the reference's own code need it; nothing else does)
+REF_SRC = pathlib.Path(os.environ["EXACTDIAG_REF_SRC"]) if os.environ.get("EXACTDIAG_REF_SRC") else None
 
 TERMS = ("tl", "tr", "jl", "jr")
 OPS = {"Szq": 0, "spectral_function_minus": 1, "spectral_function_plus": 2, "current_rung": 3, "current_leg": 4}
@@ -47,8 +49,10 @@ def build(ref: bool | None = None) -> None:
     """Compile the C restatement and, when the reference tree exists, oracle/_ref."""
     subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
     if ref is None:
-        ref = REF_SRC.is_dir()
+        ref = REF_SRC is not None and REF_SRC.is_dir()
     if ref:
+        if REF_SRC is None:
+            raise RuntimeError("set EXACTDIAG_REF_SRC to the reference's src/exactdiag directory")
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_SRC={REF_SRC}"], check=True)
 
 

@@ -82,7 +82,8 @@ def is_real(sec: O.Sector) -> bool:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default=str(O.REF_SRC.parents[1]))
+    ap.add_argument("--ref-root", default=str(O.REF_SRC.parents[1]) if O.REF_SRC else None, required=O.REF_SRC is None,
+                    help="the reference checkout (default: two levels above EXACTDIAG_REF_SRC)")
     args = ap.parse_args()
     ref_root = pathlib.Path(args.ref_root)
     O.build(ref=True)

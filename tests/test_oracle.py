@@ -98,11 +98,10 @@ def test_oracle_excitations_match_golden(oracle, golden_excitations):
 
 
 def test_oracle_bit_exact_against_reference_code(oracle):
-    if not oracle.REF_SRC.is_dir():
-        pytest.skip("reference tree absent: oracle/_ref cannot be built here")
-    oracle.build(ref=True)
+    if oracle.ref_lib() is None and oracle.REF_SRC is not None and oracle.REF_SRC.is_dir():
+        oracle.build(ref=True)
     if oracle.ref_lib() is None:
-        pytest.skip("oracle/_ref not built")
+        pytest.skip("oracle/_ref not built (EXACTDIAG_REF_SRC unset and no prebuilt library)")
     for key in [(4, 2, 3, 1, 0), (5, 2, 4, 2, 1), (6, 0, 6, 1, 1), (6, 3, 4, 0, 0), (7, 1, 6, 3, 1)]:
         sec = oracle.Sector(*key)
         a = oracle.basis(sec)

@@ -1,8 +1,9 @@
 """GPU: the allocation-free projection entry point against the allocating one.
 
 ed_project_out_noalloc exists for callers that cannot let the library call cudaMalloc during a
-call: code being captured into a CUDA graph, and services running under a fixed device-memory
-budget or their own allocator.  It keeps its scratch in a fixed device array (k <= 256 vectors).
+call: services running under a fixed device-memory budget or their own allocator, and callers that
+may not synchronise the device mid-work.  It keeps its scratch in a fixed device array (k <= 256
+vectors).
 This file is collected last so that a failing run has already run every other test; it also
 passes on its own in a fresh process.
 """

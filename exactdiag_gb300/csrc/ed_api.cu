@@ -231,7 +231,7 @@ int ed_hv(const ed_sector* h, const double weights[4], int dtype, const void* x_
     if (h->s.view.n == 0) return ED_OK;  // empty sector: nothing to read or write (the vectors may be NULL)
     if (!x_dev || !y_dev) return set_error(ED_ERR_INVALID, "ed_hv: NULL argument");
     if (x_dev == y_dev) return set_error(ED_ERR_INVALID, "ed_hv: x and y must not alias");
-    return hv_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
+    return hv_step_launch(h->s, w, dtype, x_dev, y_dev, (cudaStream_t)stream);
 }
 
 int ed_hv_mode(const ed_sector* h, const double weights[4], int dtype, const void* x_dev, void* y_dev, int mode,

@@ -622,7 +622,8 @@ int single_setup(Sector& s) {
     cudaMemcpy(s.d_hv_first.p, plan.hv_first.data(), sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(s.d_hv_count.p, plan.hv_count.data(), sizeof(int), cudaMemcpyHostToDevice);
     const int slots = std::max(std::max(count, nhv), 1);
-    if (!s.d_partials.alloc((int64_t)slots * kReduceSlots)) return set_error(ED_ERR_NOMEM, "sector reduction scratch");
+    if (!s.d_partials.alloc((int64_t)slots * kReduceSlots) || !s.d_hv_scal.alloc(8))
+        return set_error(ED_ERR_NOMEM, "sector reduction scratch");
     // stabiliser blocks' expanded copies: allocated here, once, for the widest element (complex
     // double, which a real sector also accepts), so that no step allocates (steps may be captured
     // in a CUDA graph)
@@ -711,6 +712,13 @@ int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext
     }
     ED_CHECK_LAUNCH("lanczos_update_kernel");
     return ED_OK;
+}
+
+// y = H x through the step kernels (the step's first pass: no previous vector; its scalars go to a
+// per-sector scratch nobody reads).
+int hv_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st) {
+    if (s.view.n == 0) return ED_OK;
+    return lanczos_hv_launch(s, w, dtype, x, nullptr, y, s.d_hv_scal.p, nullptr, st);
 }
 
 int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,

@@ -147,6 +147,7 @@ struct Sector {
     DevBuf<uint64_t> d_keys;
     DevBuf<uint8_t> d_orbit;
     DevBuf<double> d_partials;   // [hv_grid][kReduceSlots] scratch of the fused Lanczos step
+    DevBuf<double> d_hv_scal;    // step scalars written by ed_hv's pass through the step kernels (unused)
     DevBuf<double> d_proj;       // projection scratch: partial dots and coefficients
     // the sector as a batch of one (step kernels): device view, offsets and chunk table
     int n_chunks = 0;
@@ -227,6 +228,7 @@ struct HvWeights {
     int faithful;  // 1: every term through the reference-faithful orbit walk (self-check path)
 };
 int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st);
+int hv_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, void* y, cudaStream_t st);
 int lanczos_step_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev,
                         void* vnext, double* scal, double* partials, cudaStream_t st);
 int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* v, const void* vprev, void* vnext,

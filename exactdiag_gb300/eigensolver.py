@@ -107,18 +107,11 @@ class _Krylov:
         return out
 
 
-def lowest_eigenpairs(sector: DeviceSector, weights, k: int, precision: str = "fp64", tol: float = 1e-10,
-                      max_krylov: int = 300, seed: int = 0, memory_fraction: float = 0.5):
-    """(eigenvalues[k], eigenvectors (n, k) complex128 on the host) of the sector's H."""
+def _lowest(sector: DeviceSector, weights, k: int, dt: torch.dtype, tol: float, max_krylov: int, seed: int,
+            memory_fraction: float):
+    """Deflated Lanczos rounds until k eigenpairs are locked and a confirmation run finds nothing lower:
+    (eigenvalues in the order found, the locked vectors (k + 1, n) of dtype dt)."""
     n = sector.n
-    if n == 0:
-        return np.zeros(0), np.zeros((0, 0), np.complex128)
-    dt = sector.dtype(precision)
-    if n < 250 or n < 2 * (k + 4):
-        h = dense_matrix(sector, weights, dt)
-        vals, vecs = np.linalg.eigh(h)
-        return vals[:k], vecs[:, :k]
-    k = min(k, n)
     elem = torch.empty(0, dtype=dt).element_size()
     free, _ = torch.cuda.mem_get_info(sector.device)
     m_cap = int(memory_fraction * free / (n * elem)) - k - 2
@@ -156,6 +149,51 @@ def lowest_eigenpairs(sector: DeviceSector, weights, k: int, precision: str = "f
             vals.append(float(theta[q]))
         if rounds > 4 * k + 4:
             break
+    return vals, locked
+
+
+def lowest_eigenpairs(sector: DeviceSector, weights, k: int, precision: str = "fp64", tol: float = 1e-10,
+                      max_krylov: int = 300, seed: int = 0, memory_fraction: float = 0.5, fp32_tol: float = 1e-6,
+                      refine_krylov: int = 120):
+    """(eigenvalues[k], eigenvectors (n, k) complex128 on the host) of the sector's H.
+
+    precision "fp64": FP64 (complex128) Krylov vectors throughout.
+    precision "mixed": the eigenpairs are first found with FP32 (complex64) Krylov vectors and FP64
+    dot products to `fp32_tol`; each is then refined by an FP64 Lanczos run started from its FP32
+    vector, in the complement of the eigenvectors already refined, to `tol`.
+    """
+    n = sector.n
+    if n == 0:
+        return np.zeros(0), np.zeros((0, 0), np.complex128)
+    if n < 250 or n < 2 * (k + 4):
+        h = dense_matrix(sector, weights, sector.dtype("fp64"))
+        vals, vecs = np.linalg.eigh(h)
+        return vals[:k], vecs[:, :k]
+    k = min(k, n)
+    if precision != "mixed":
+        vals, locked = _lowest(sector, weights, k, sector.dtype("fp64"), tol, max_krylov, seed, memory_fraction)
+    else:
+        vals32, locked32 = _lowest(sector, weights, k, sector.dtype("fp32"), fp32_tol, max_krylov, seed,
+                                   memory_fraction)
+        dt = sector.dtype("fp64")
+        order32 = np.argsort(vals32)[:k]
+        free, _ = torch.cuda.mem_get_info(sector.device)
+        elem = torch.empty(0, dtype=dt).element_size()
+        m_cap = int(memory_fraction * free / (n * elem)) - k - 2
+        kry = _Krylov(sector, weights, dt, max(8, min(refine_krylov, n - 1, m_cap)))
+        locked = torch.zeros(k + 1, n, dtype=dt, device=sector.device)
+        norm = torch.zeros(1, dtype=torch.float64, device=sector.device)
+        vals = []
+        for j, i in enumerate(order32):
+            m, theta, vecs = kry.run(locked32[int(i)].to(dt), locked, j, 1, tol, check_every=4)
+            row = locked[j]
+            row.copy_(kry.ritz_vectors(m, vecs, [0])[0].to(dt))
+            for _ in range(2):
+                if j:
+                    sector.project_out(locked, j, row)
+            sector.normalize(row, norm)
+            vals.append(float(theta[0]))
+        del locked32
     order = np.argsort(vals)[:k]
     out_vals = np.array(vals)[order]
     out_vecs = locked[torch.as_tensor(order, device=sector.device)].to(torch.complex128).cpu().numpy().T

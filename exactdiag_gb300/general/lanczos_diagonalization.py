@@ -50,8 +50,9 @@ def calculate_eigenpairs(config):
         _logger.warning("hamiltonian has 0 rows, skipping eigen problem")
         return [], []
     k = config.eigenpair.num_eigenpairs
-    # eigenpairs are always solved with FP64 vectors; "mixed" applies to the spectrum recursions
-    eigvals, eigvecs = lowest_eigenpairs(hamiltonian.sector, hamiltonian.weights_tuple, k, precision="fp64")
+    # "mixed": FP32 Krylov vectors with FP64 reductions, each eigenpair refined in FP64 (eigensolver)
+    eigvals, eigvecs = lowest_eigenpairs(hamiltonian.sector, hamiltonian.weights_tuple, k,
+                                         precision=hamiltonian.precision)
     eigvals = np.real(eigvals)
     order = eigvals.argsort()[:k]
     return eigvals[order], eigvecs[:, order]

@@ -93,17 +93,115 @@ def ritz_vector(run: LanczosRun, v0: torch.Tensor, coeffs: np.ndarray) -> torch.
     return acc
 
 
-def ground_state(sector: DeviceSector, weights, num_steps: int, precision: str = "mixed", seed: int = 0,
-                 refine_steps: int = 32, v0: torch.Tensor | None = None, use_graph: bool = True) -> dict:
-    """Ground energy of a sector.
-
-    precision "fp64": plain FP64 Lanczos; E0 = lowest Ritz value.
-    precision "mixed": FP32 (complex64) Lanczos vectors with FP64 reductions;
-    the lowest Ritz vector is rebuilt in FP64 on a second pass and refined by
-    `refine_steps` FP64 Lanczos steps started from it (Rayleigh quotient and
-    residual come from that refinement run).
-    """
+def _lowest_ritz(a: np.ndarray, b_next: np.ndarray):
+    """Lowest eigenpair of the tridiagonal matrix (diagonal a, off-diagonal b_next[:-1])."""
     from scipy.linalg import eigh_tridiagonal
+
+    if len(a) == 1:
+        return float(a[0]), np.ones(1)
+    w, s = eigh_tridiagonal(a, b_next[: len(a) - 1], select="i", select_range=(0, 0))
+    return float(w[0]), s[:, 0]
+
+
+class CheckedLanczos:
+    """A ground-state Lanczos recursion that reads its coefficients every `check_every` steps and
+    stops once the lowest Ritz value changes by at most `tol` (relative) over a window, on breakdown,
+    or after `max_steps`.  With `store`, every Lanczos vector is kept (one extra vector of the run's
+    dtype per step) so that the Ritz vector needs no second pass; otherwise two buffers rotate."""
+
+    def __init__(self, sector: DeviceSector, weights, dtype: torch.dtype, max_steps: int, store: bool):
+        from exactdiag_gb300 import autotune
+
+        self.sector, self.weights, self.dtype = sector, weights_tuple(weights), dtype
+        self.max_steps = int(max_steps)
+        self.store = store
+        dev = sector.device
+        # kept vectors are allocated as the recursion reaches them
+        self.V = [torch.zeros(sector.n, dtype=dtype, device=dev) for _ in range(2)]
+        self.scal = torch.zeros(2 * self.max_steps + 4, dtype=torch.float64, device=dev)
+        self.norm = torch.zeros(1, dtype=torch.float64, device=dev)
+        autotune.ensure(sector, self.weights, dtype)
+
+    def _buf(self, k: int) -> torch.Tensor:
+        if not self.store:
+            return self.V[k % 2]
+        while len(self.V) <= k:
+            self.V.append(torch.empty_like(self.V[0]))
+        return self.V[k]
+
+    def run(self, v0: torch.Tensor, tol: float, check_every: int = 10, min_steps: int = 2) -> dict:
+        s = self.sector
+        self.V[0].copy_(v0)
+        s.normalize(self.V[0], self.norm)
+        self.scal.zero_()
+        theta_prev, steps = None, self.max_steps
+        for k in range(self.max_steps):
+            v, nxt = self._buf(k), self._buf(k + 1)
+            s.lanczos_step(self.weights, v, self._buf(k - 1) if k > 0 else None, nxt, self.scal[2 * k: 2 * k + 4])
+            m = k + 1
+            if m % check_every and m != self.max_steps:
+                continue
+            x = self.scal[: 2 * m + 2].cpu().numpy()
+            a, b_next = x[1: 2 * m: 2], x[2: 2 * m + 1: 2]
+            small = np.nonzero(b_next < 1e-8)[0]
+            if len(small):
+                steps = int(small[0]) + 1
+                break
+            theta, _ = _lowest_ritz(a, b_next)
+            if m >= min_steps and theta_prev is not None and abs(theta - theta_prev) <= tol * abs(theta):
+                steps = m
+                break
+            theta_prev = theta
+        x = self.scal[: 2 * steps + 2].cpu().numpy()
+        self.a, self.b_next = x[1: 2 * steps: 2].copy(), x[2: 2 * steps + 1: 2].copy()
+        self.steps = steps
+        self.theta, self.s = _lowest_ritz(self.a, self.b_next)
+        self.residual = abs(float(self.b_next[steps - 1]) * float(self.s[-1]))
+        return {"theta": self.theta, "steps": steps, "residual": self.residual}
+
+    def ritz_vector(self, v0: torch.Tensor) -> torch.Tensor:
+        """The lowest Ritz vector in FP64 (complex128 for complex sectors): from the stored vectors,
+        else by a second, bitwise-identical pass from v0."""
+        s = self.sector
+        acc = torch.zeros(s.n, dtype=torch.float64 if s.is_real else torch.complex128, device=s.device)
+        if self.store:
+            for k in range(self.steps):
+                s.accumulate(self.V[k], complex(self.s[k]), acc)
+            return acc
+        self.V[0].copy_(v0)
+        s.normalize(self.V[0], self.norm)
+        scal = torch.zeros_like(self.scal)
+        for k in range(self.steps):
+            v, nxt = self._buf(k), self._buf(k + 1)
+            s.accumulate(v, complex(self.s[k]), acc)
+            if k + 1 < self.steps:
+                s.lanczos_step(self.weights, v, self._buf(k - 1) if k > 0 else None, nxt, scal[2 * k: 2 * k + 4])
+        return acc
+
+
+def _vectors_that_fit(sector: DeviceSector, dtype: torch.dtype, fraction: float = 0.6) -> int:
+    """How many vectors of dtype fit in `fraction` of the device memory that is free (blocks that
+    torch holds in its cache but does not use count as free)."""
+    elem = torch.empty(0, dtype=dtype).element_size()
+    free, _ = torch.cuda.mem_get_info(sector.device)
+    cached = torch.cuda.memory_reserved(sector.device) - torch.cuda.memory_allocated(sector.device)
+    return int(fraction * (free + cached) / max(1, sector.n * elem))
+
+
+def ground_state(sector: DeviceSector, weights, max_steps: int = 240, precision: str = "mixed", seed: int = 0,
+                 v0: torch.Tensor | None = None, tol: float = 1e-13, fp32_tol: float = 1e-7,
+                 refine_max: int = 160, check_every: int = 10, store: bool | None = None) -> dict:
+    """Ground energy of a sector, each form run until its lowest Ritz value has converged.
+
+    precision "fp64": plain FP64 Lanczos until the lowest Ritz value changes by at most `tol`
+    (relative) over `check_every` steps.
+    precision "mixed": FP32 (complex64) Lanczos with FP64 reductions until the Ritz value changes by
+    at most `fp32_tol` (the FP32 vectors' resolution); the Ritz vector is accumulated in FP64 from the
+    kept FP32 Lanczos vectors (a second pass when they do not fit in device memory) and refined by
+    FP64 Lanczos started from it, until its Ritz value changes by at most `tol`.  E0 is the refined
+    value; the result also carries the step counts and the wall time of each phase.
+    """
+    import time
 
     dt = sector.dtype("fp64" if precision == "fp64" else "fp32")
     if v0 is None:
@@ -111,25 +209,37 @@ def ground_state(sector: DeviceSector, weights, num_steps: int, precision: str =
         v0 = torch.as_tensor(x, device=sector.device).to(dt)
     else:
         v0 = v0.to(device=sector.device, dtype=dt)
-    run = LanczosRun(sector, weights, num_steps, dt)
-    run.run(v0, use_graph=use_graph)
-    a, b, _ = run.coefficients()
-    if len(a) == 1:
-        theta, vecs = np.array([a[0]]), np.ones((1, 1))
-    else:
-        theta, vecs = eigh_tridiagonal(a, b[1:])
-    out = {"theta": float(theta[0]), "a": a, "b": b, "steps": len(a), "E0": float(theta[0])}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     if precision == "fp64":
-        return out
-    psi = ritz_vector(run, v0, vecs[:, 0])
-    ref = LanczosRun(sector, weights, refine_steps, psi.dtype)
-    ref.run(psi, use_graph=False)
-    ra, rb, _ = ref.coefficients()
-    rq = float(ra[0])
-    resid = float(rb[1]) if len(rb) > 1 else 0.0
-    e_ref = float(tridiagonal_eigvals(ra, rb)[0])
-    out.update({"E0": e_ref, "rayleigh": rq, "residual": resid, "refine_steps": len(ra)})
-    return out
+        run = CheckedLanczos(sector, weights, dt, max_steps, store=False)
+        r = run.run(v0, tol, check_every)
+        torch.cuda.synchronize()
+        return {"E0": r["theta"], "theta": r["theta"], "steps": r["steps"], "residual": r["residual"],
+                "a": run.a, "time_s": time.perf_counter() - t0}
+    steps32 = max_steps
+    if store is None:
+        # keep the FP32 vectors when at least 100 of them fit; the FP32 stage then stops where they run
+        # out at the latest (the refinement takes the rest of the convergence)
+        cap = _vectors_that_fit(sector, dt) - 1
+        keep = cap >= 100
+        if keep:
+            steps32 = min(max_steps, cap)
+    else:
+        keep = store
+    run = CheckedLanczos(sector, weights, dt, steps32, store=keep)
+    r = run.run(v0, fp32_tol, check_every)
+    psi = run.ritz_vector(v0)
+    del run
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ref = CheckedLanczos(sector, weights, psi.dtype, refine_max, store=False)
+    rr = ref.run(psi, tol, check_every=4)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"E0": rr["theta"], "theta": r["theta"], "steps": r["steps"], "refine_steps": rr["steps"],
+            "residual": rr["residual"], "rayleigh": float(ref.a[0]), "kept_vectors": keep,
+            "time_s": t2 - t0, "time_fp32_s": t1 - t0, "time_refine_s": t2 - t1}
 
 
 def lanczos_coefficients(sector: DeviceSector, weights, v0: torch.Tensor, num_lanczos_vecs: int,

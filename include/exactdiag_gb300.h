@@ -88,11 +88,12 @@ int ed_basis_export(const ed_sector* s, int64_t* sparse_dev, int32_t* orbit_dev,
  * dtype is ED_F64/ED_C128/ED_F32/ED_C64; real dtypes require a real sector. */
 int ed_hv(const ed_sector* s, const double weights[4], int dtype, const void* x_dev, void* y_dev, void* stream);
 
-/* ed_hv with a choice of row algorithm: mode 0 is ed_hv (per-block descriptors: colex-rank
- * deltas inside blocks whose hole pattern has a trivial stabiliser, precomputed coset
- * permutations elsewhere); mode 1 resolves every term with the reference-faithful orbit walk
- * (get_symmetry_states_from_state, symmetry_ladder.h:113-235).  Both give the same operator; mode 1
- * is the self-check of mode 0 at sizes the CPU oracle cannot reach. */
+/* H x by one of two independent row algorithms, as self-checks of ed_hv (which runs the fused
+ * step kernels: segments of free blocks, expanded copies of stabiliser blocks): mode 0 one thread
+ * per row with per-block descriptors (colex-rank deltas inside blocks whose hole pattern has a
+ * trivial stabiliser, precomputed coset permutations elsewhere); mode 1 every term through the
+ * reference-faithful orbit walk (get_symmetry_states_from_state, symmetry_ladder.h:113-235).  All
+ * three give the same operator; mode 1 checks the others at sizes the CPU oracle cannot reach. */
 int ed_hv_mode(const ed_sector* s, const double weights[4], int dtype, const void* x_dev, void* y_dev, int mode,
                void* stream);
 

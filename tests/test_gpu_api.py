@@ -113,6 +113,40 @@ def test_eigenpairs_vs_oracle(torch, oracle, key):
         assert np.linalg.norm(h @ v - vals[i] * v) < 1e-6
 
 
+@pytest.mark.parametrize("key", [(8, 2, 7, 0, 0), (7, 2, 6, 2, 1), (10, 2, 9, 3, 1)])
+def test_mixed_eigenpairs_match_fp64(torch, oracle, key):
+    """precision "mixed" (FP32 Krylov vectors, FP64 reductions, each eigenpair refined in FP64) gives
+    the FP64 eigenvalues to 1e-10 relative and FP64-accurate eigenvectors."""
+    from exactdiag_gb300.eigensolver import lowest_eigenpairs
+
+    sec = _sector(key)
+    v64, _ = lowest_eigenpairs(sec, W, 4)
+    vmx, vecs = lowest_eigenpairs(sec, W, 4, precision="mixed")
+    assert np.max(np.abs(vmx - v64) / np.abs(v64)) < 1e-10, (vmx, v64)
+    if key[0] <= 8:
+        osec = oracle.Sector(*key)
+        h = oracle.hamiltonian(osec, W, oracle.basis(osec))
+        for i in range(4):
+            assert np.linalg.norm(h @ vecs[:, i] - vmx[i] * vecs[:, i]) < 1e-6
+
+
+def test_drop_in_calculate_eigenpairs_mixed(torch, in_tmp):
+    """Hamiltonian_Config.precision = "mixed" reaches the mixed eigen-solver through the reference's
+    own entry point (general/lanczos_diagonalization.py: calculate_eigenpairs)."""
+    from exactdiag_gb300.general import lanczos_diagonalization as ld
+    from exactdiag_gb300.tJ_spin_half_ladder import configs
+
+    out = {}
+    for precision in ("fp64", "mixed"):
+        cfg = configs.Eigenpair_Config(hamiltonian={"num_rungs": 8, "num_holes": 2, "weights": W,
+                                                    "symmetry_qs": {"leg": 0, "rung": 0}, "num_threads": 1,
+                                                    "precision": precision},
+                                       eigenpair={"num_eigenpairs": 4})
+        out[precision] = ld.calculate_eigenpairs(cfg)[0]
+    assert np.max(np.abs(out["mixed"] - out["fp64"])) < 1e-9
+    assert np.max(np.abs(out["fp64"] - np.array([-10.12086831, -9.85429876, -9.70467762, -9.63624331]))) < 6e-9
+
+
 def test_config1_lowest_four(torch):
     # 2x8 ladder, 2 holes, k=(0,0): known answer of the reference's own stored H (FP64 eigsh, tol 1e-14)
     from exactdiag_gb300.eigensolver import lowest_eigenpairs

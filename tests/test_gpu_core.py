@@ -182,20 +182,29 @@ def test_hv_hermitian_full_size(torch, key):
                                  (10, 1, 9, 3, 0), (8, 0, 8, 2, 1), (12, 2, 11, 0, 0), (12, 2, 11, 6, 1),
                                  (12, 2, 11, 5, 0), (11, 3, 9, 2, 1)])
 def test_fast_rows_equal_faithful_orbit_walk(torch, key):
-    """The descriptor-driven rows (colex deltas, coset permutations) against the reference-faithful walk."""
+    """The descriptor-driven rows (colex deltas, coset permutations) and the fused step kernels
+    (ed_hv: segments, expanded copies) against the reference-faithful walk."""
     sec = _sector(key)
     x = _to_dev(torch, seeded_vector(sec.n, 41, not sec.is_real), sec, "fp64")
     y_fast = sec.hv_mode(x, W, 0)
+    y_step = sec.hv(x, W)
     y_walk = sec.hv_mode(x, W, 1)
     scale = float(torch.max(torch.abs(y_walk)).item())
     assert float(torch.max(torch.abs(y_fast - y_walk)).item()) < 1e-12 * max(1.0, scale)
+    assert float(torch.max(torch.abs(y_step - y_walk)).item()) < 1e-12 * max(1.0, scale)
 
 
 def test_fast_rows_equal_faithful_orbit_walk_2x14(torch):
-    """Full-size check of the fast rows on the spec sector (1.4e8 rows), FP64."""
+    """Full-size check of the fast rows and of the fused step kernels on the 2x14 two-hole sector
+    (1.4e8 rows), FP64; and of the FP32 step kernels against the FP64 walk at FP32 resolution."""
     sec = _sector((14, 2, 13, 0, 0))
     g = torch.Generator(device="cuda").manual_seed(7)
     x = torch.rand(sec.n, dtype=torch.float64, device="cuda", generator=g) - 0.5
-    y_fast = sec.hv_mode(x, W, 0)
     y_walk = sec.hv_mode(x, W, 1)
-    assert float(torch.max(torch.abs(y_fast - y_walk)).item()) < 1e-12 * float(torch.max(torch.abs(y_walk)).item())
+    scale = float(torch.max(torch.abs(y_walk)).item())
+    y = sec.hv_mode(x, W, 0)
+    assert float(torch.max(torch.abs(y - y_walk)).item()) < 1e-12 * scale
+    y = sec.hv(x, W)
+    assert float(torch.max(torch.abs(y - y_walk)).item()) < 1e-12 * scale
+    y = sec.hv(x.float(), W)
+    assert float(torch.max(torch.abs(y.double() - y_walk)).item()) < 2e-5 * scale

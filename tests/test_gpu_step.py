@@ -1,8 +1,9 @@
-"""GPU: the fused Lanczos step kernels (one per block kind) against the plain H.v kernel.
+"""GPU: the fused Lanczos step kernels (one per block kind) against the one-thread-per-row H.v kernel.
 
 ed_lanczos_hv with no previous vector writes y = H v and the step's partial sums; y must equal
-ed_hv's H v (which the core tests pin to the oracle and to the reference-faithful orbit walk), and
-<v, Hv> must equal the FP64 dot product of the two vectors.
+ed_hv_mode(..., 0)'s H v (an independent row algorithm, pinned by the core tests to the oracle and
+to the reference-faithful orbit walk), and <v, Hv> must equal the FP64 dot product of the two
+vectors.
 """
 
 import numpy as np
@@ -29,7 +30,7 @@ def _check(torch, key, precision, tol, w=W):
     dt = sec.dtype(precision)
     x = seeded_vector(sec.n, 17, not sec.is_real)
     v = torch.as_tensor(x if not sec.is_real else x.real, device=sec.device).to(dt)
-    ref = sec.hv(v, w)
+    ref = sec.hv_mode(v, w, 0)
     y = torch.zeros_like(v)
     scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
     sec.lanczos_hv(w, v, None, y, scal[0:4])

@@ -84,11 +84,12 @@ def kind_rows(sector: DeviceSector) -> tuple[int, int, int]:
 
 
 def step_launches(sector: DeviceSector) -> int:
-    """Kernel launches of one ed_lanczos_step: one fused H.v kernel per row kind present, the
-    expansion of the stabiliser blocks when there are any, the scalar reduction, and the update
-    (flat pass, exact-norm pass, exact b, scaling pass)."""
-    kinds = row_kinds(sector)
-    return sum(1 for c in kinds if c > 0) + (1 if kinds[1] > 0 else 0) + 1 + 4
+    """Kernel launches of one ed_lanczos_step (ed_sector_step_launches): the expanded copies when
+    the sector has any, one fused H.v kernel per row kind present, the scalar reduction, and the
+    update (flat pass, exact-norm pass, exact b, scaling pass)."""
+    c = ctypes.c_int()
+    nat.check("ed_sector_step_launches", sector._lib.ed_sector_step_launches(sector.handle, ctypes.byref(c)))
+    return int(c.value)
 
 
 _MEMO: dict = {}
@@ -105,14 +106,20 @@ def ensure(sector: DeviceSector, weights, dtype: torch.dtype) -> dict | None:
     rec = _MEMO.get(key)
     if rec is None:
         rec = tune(sector, weights, dtype)
-        _MEMO[key] = rec
     else:
         set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
     return rec
 
 
 def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_cache: bool = True) -> dict:
-    """Apply the fastest launch configuration for this sector shape; returns the record used."""
+    """Apply the fastest launch configuration for this sector shape; returns the record used (also
+    kept in this process's memo, which ensure() reads)."""
+    rec = _tune(sector, weights, dtype, steps, use_cache)
+    _MEMO[_key(sector, dtype)] = rec
+    return rec
+
+
+def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cache: bool) -> dict:
     key = _key(sector, dtype)
     cache = _load() if use_cache else {}
     if key in cache:

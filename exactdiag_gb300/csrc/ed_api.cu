@@ -2,6 +2,7 @@
 // Every entry point validates its arguments, returns an int status and never
 // lets a C++ exception or CUDA error escape; the text of the last failure is
 // kept per thread for ed_last_error_string().
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -63,6 +64,8 @@ int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out) {
     ed_sector* h = new (std::nothrow) ed_sector();
     if (!h) return set_error(ED_ERR_NOMEM, "ed_sector_create: host allocation");
     Sector& s = h->s;
+    static std::atomic<uint64_t> next_serial{1};
+    s.serial = next_serial.fetch_add(1);
     uint32_t comb[kCombStride][kCombStride];
     host_comb(comb);
     SectorView& V = s.view;
@@ -105,6 +108,7 @@ int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out) {
 }
 
 int ed_sector_destroy(ed_sector* h) {
+    if (h) batch_forget(h->s);
     delete h;
     return ED_OK;
 }
@@ -177,6 +181,16 @@ int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
     counts[0] = h->s.kind_count[kRowsFree];
     counts[1] = h->s.kind_count[kRowsCand];
     counts[2] = h->s.kind_count[kRowsGeneric];
+    return ED_OK;
+}
+
+int ed_sector_step_launches(const ed_sector* h, int* launches) {
+    if (!h || !launches) return set_error(ED_ERR_INVALID, "ed_sector_step_launches: NULL argument");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_step_launches: basis not built");
+    const Sector& s = h->s;
+    int n = s.n_tasks > 0 ? 1 : 0;  // expanded copies
+    for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind) n += s.kind_count[kind] > 0 ? 1 : 0;
+    *launches = n + 1 + 4;  // + scalars; update: flat pass, exact-norm pass, exact b, scaling pass
     return ED_OK;
 }
 

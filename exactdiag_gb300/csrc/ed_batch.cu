@@ -6,12 +6,15 @@
 // general/cython_lanczos_diagonalization.pyx:50-77) run together.  The rows of
 // all sectors are cut into chunks; each phase of a step is one launch over all
 // chunks (fused H.v with per-chunk FP64 partial sums, per-sector scalars, the
-// in-place update), and the m steps are captured once into a CUDA graph that is
-// launched once.  The sectors of one batch share L, Nh and Nd (one set of
-// shared-memory tables); they differ in momentum and dimension.
+// in-place update), and the m steps are captured once into a CUDA graph.  The
+// workspace and the instantiated graph are kept for the next call of the same
+// batch shape, which only copies its start vectors in and replays the graph.
+// The sectors of one batch share L, Nh and Nd (one set of shared-memory
+// tables); they differ in momentum and dimension.
 //
 // Projection (full reorthogonalisation for the lowest-eigenpair solver):
 // w <- w - sum_j <v_j, w> v_j with FP64 dot products.
+#include <mutex>
 #include <vector>
 
 #include "ed_step.cuh"
@@ -455,117 +458,226 @@ static int dtype_code(bool dbl, bool cplx) { return dbl ? (cplx ? ED_C128 : ED_F
 
 static int update_grid(const Sector& s, int nchunks) { return std::max(1, std::min(nchunks, s.num_sms * 8)); }
 
+namespace {
+
+// A batch's device workspace (tables, both vector buffers of every sector, reduction scratch, the
+// expanded copies, the step scalars) and its instantiated step graph, kept for the next call of the
+// same shape: the same sectors in the same order on the same device, dtype, m, weights, graph use
+// and launch shape.  Repeated recursions of one batch (one per degenerate ground state, or a sweep
+// of start vectors) then plan, allocate and capture once.  One workspace is kept: a call of another
+// shape replaces it, and destroying one of its sectors frees it (batch_forget).
+struct BatchWorkspace {
+    std::vector<uint64_t> serials;
+    int device = -1, dtype = -1, m = 0, use_graph = 0;
+    HvWeights w{};
+    int minb = 0, hv_grid = 0, other_grid = 0, cand_grid = 0;
+    int nsec = 0, nchunks = 0, nhv = 0, ntasks = 0, stride = 0, grid = 0;
+    size_t smem = 0;
+    int64_t total = 0;
+    int kind_first[4] = {0, 0, 0, 0}, kind_count[4] = {0, 0, 0, 0};
+    std::vector<int64_t> hoffs, hn;
+    DevBuf<SectorView> dviews;
+    DevBuf<int64_t> doffs;
+    DevBuf<BatchChunk> dchunks, dhv;
+    DevBuf<int> dkidx, dcfirst, dccount, dhfirst, dhcount;
+    DevBuf<double> partials, coef;
+    DevBuf<uint8_t> buf0, buf1, xfull;
+    DevBuf<ExpandTask> dtasks;
+    cudaStream_t priv = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~BatchWorkspace() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (priv) cudaStreamDestroy(priv);
+    }
+    bool matches(const std::vector<const Sector*>& secs, int dev, int dt, int mm, const HvWeights& ww,
+                 int graph) const {
+        if (dev != device || dt != dtype || mm != m || graph != use_graph || secs.size() != serials.size())
+            return false;
+        for (size_t i = 0; i < secs.size(); ++i)
+            if (secs[i]->serial != serials[i]) return false;
+        for (int t = 0; t < 4; ++t)
+            if (ww.w[t] != w.w[t]) return false;
+        const Sector& s0 = *secs[0];
+        return ww.faithful == w.faithful && s0.hv_minb == minb && s0.hv_grid == hv_grid &&
+               s0.other_grid == other_grid && s0.cand_grid_f32 == cand_grid;
+    }
+};
+
+std::mutex g_batch_mu;
+BatchWorkspace* g_batch = nullptr;  // left to the driver at process exit (no CUDA calls from static destructors)
+
+void drop_batch_workspace() {
+    if (!g_batch) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != g_batch->device) cudaSetDevice(g_batch->device);
+    delete g_batch;
+    g_batch = nullptr;
+    cudaSetDevice(cur);
+}
+
+}  // namespace
+
+void batch_forget(const Sector& s) {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    if (!g_batch) return;
+    for (uint64_t id : g_batch->serials)
+        if (id == s.serial) {
+            drop_batch_workspace();
+            return;
+        }
+}
+
+// Plans the batch, allocates its workspace and uploads the tables (no vector data yet).
 template <typename R, bool CPLX>
-static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& w, const void* const* v0, int m,
-                       double* coef, int use_graph, cudaStream_t st) {
+static int batch_prepare(BatchWorkspace& W, const std::vector<const Sector*>& secs, int m, cudaStream_t st) {
     const int nsec = (int)secs.size();
     const size_t esz = sizeof(typename Vec<R, CPLX>::T);
     std::vector<SectorView> hviews(nsec);
-    std::vector<int64_t> hoffs(nsec);
     ChunkPlan plan;
     plan_chunks(secs, plan);
-    int64_t total = 0;
+    W.nsec = nsec;
+    W.hoffs.assign(nsec, 0);
+    W.hn.assign(nsec, 0);
+    W.total = 0;
     for (int s = 0; s < nsec; ++s) {
         hviews[s] = secs[s]->view;
-        hoffs[s] = total;
-        total += hviews[s].n;
+        W.hoffs[s] = W.total;
+        W.hn[s] = hviews[s].n;
+        W.total += hviews[s].n;
     }
-    const int nchunks = (int)plan.chunks.size();
-    const int nhv = (int)plan.hv.size();
-    const int stride = 2 * m + 4;
-    DevBuf<SectorView> dviews(nsec);
-    DevBuf<int64_t> doffs(nsec);
-    DevBuf<BatchChunk> dchunks(nchunks), dhv(nhv);
-    DevBuf<int> dkidx(nhv);
-    DevBuf<int> dcfirst(nsec), dccount(nsec), dhfirst(nsec), dhcount(nsec);
-    DevBuf<double> partials((int64_t)std::max(nchunks, nhv) * kReduceSlots);
-    DevBuf<uint8_t> buf0((int64_t)(total * esz)), buf1((int64_t)(total * esz));
-    const int ntasks = (int)plan.tasks.size();
-    DevBuf<ExpandTask> dtasks(ntasks);
-    DevBuf<uint8_t> xfull((int64_t)(plan.n_full * (int64_t)esz));
-    if (!dviews.ok() || !doffs.ok() || !dchunks.ok() || !dhv.ok() || !dkidx.ok() || !dcfirst.ok() || !dccount.ok() ||
-        !dhfirst.ok() || !dhcount.ok() || !partials.ok() || !buf0.ok() || !buf1.ok() || !dtasks.ok() || !xfull.ok())
-        return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
-    if (ntasks)
-        cudaMemcpyAsync(dtasks.p, plan.tasks.data(), ntasks * sizeof(ExpandTask), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(doffs.p, hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dchunks.p, plan.chunks.data(), nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
-    if (nhv) {
-        cudaMemcpyAsync(dhv.p, plan.hv.data(), nhv * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(dkidx.p, plan.kind_idx.data(), nhv * sizeof(int), cudaMemcpyHostToDevice, st);
+    W.nchunks = (int)plan.chunks.size();
+    W.nhv = (int)plan.hv.size();
+    W.ntasks = (int)plan.tasks.size();
+    W.stride = 2 * m + 4;
+    for (int kind = 0; kind < 4; ++kind) {
+        W.kind_first[kind] = plan.kind_first[kind];
+        W.kind_count[kind] = plan.kind_count[kind];
     }
-    cudaMemcpyAsync(dcfirst.p, plan.cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dccount.p, plan.ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dhfirst.p, plan.hv_first.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dhcount.p, plan.hv_count.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(coef, 0, (size_t)nsec * stride * sizeof(double), st);
-    for (int s = 0; s < nsec; ++s)
-        if (hviews[s].n)
-            cudaMemcpyAsync(buf0.p + hoffs[s] * esz, v0[s], hviews[s].n * esz, cudaMemcpyDeviceToDevice, st);
     const Sector& s0 = *secs[0];
-    const int grid = update_grid(s0, nchunks);
-    const size_t smem = hv_smem_bytes(hviews[0], sizeof(R));
-    // start vectors: |v0| and normalisation
-    norm_partials_kernel<R, CPLX><<<grid, 256, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, partials.p);
-    lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, st>>>(partials.p, dcfirst.p, dccount.p, coef, stride, 0, 1,
-                                                           stride - 1);
-    lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, st>>>(doffs.p, dchunks.p, nchunks, buf0.p, nullptr, coef,
-                                                                 stride, 0, 1, stride - 1);
-    ED_CHECK_LAUNCH("batch start vectors");
-    cudaStream_t cap = st;
-    cudaStream_t priv = nullptr;
-    if (use_graph) {
-        if (cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking) != cudaSuccess)
-            return set_error(ED_ERR_CUDA, "ed_batch_lanczos: stream");
-        cap = priv;
-        if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-            cudaStreamDestroy(priv);
-            return set_error(ED_ERR_CUDA, "ed_batch_lanczos: begin capture");
-        }
+    W.grid = update_grid(s0, W.nchunks);
+    W.smem = hv_smem_bytes(hviews[0], sizeof(R));
+    if (!W.dviews.alloc(nsec) || !W.doffs.alloc(nsec) || !W.dchunks.alloc(W.nchunks) || !W.dhv.alloc(W.nhv) ||
+        !W.dkidx.alloc(W.nhv) || !W.dcfirst.alloc(nsec) || !W.dccount.alloc(nsec) || !W.dhfirst.alloc(nsec) ||
+        !W.dhcount.alloc(nsec) || !W.partials.alloc((int64_t)std::max(W.nchunks, W.nhv) * kReduceSlots) ||
+        !W.coef.alloc((int64_t)nsec * W.stride) || !W.buf0.alloc((int64_t)(W.total * esz)) ||
+        !W.buf1.alloc((int64_t)(W.total * esz)) || !W.dtasks.alloc(W.ntasks) ||
+        !W.xfull.alloc((int64_t)(plan.n_full * (int64_t)esz)))
+        return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: workspace");
+    if (W.ntasks)
+        cudaMemcpyAsync(W.dtasks.p, plan.tasks.data(), W.ntasks * sizeof(ExpandTask), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.dviews.p, hviews.data(), nsec * sizeof(SectorView), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.doffs.p, W.hoffs.data(), nsec * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.dchunks.p, plan.chunks.data(), W.nchunks * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
+    if (W.nhv) {
+        cudaMemcpyAsync(W.dhv.p, plan.hv.data(), W.nhv * sizeof(BatchChunk), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(W.dkidx.p, plan.kind_idx.data(), W.nhv * sizeof(int), cudaMemcpyHostToDevice, st);
     }
-    uint8_t* b[2] = {buf0.p, buf1.p};
-    for (int k = 0; k < m; ++k) {
+    cudaMemcpyAsync(W.dcfirst.p, plan.cfirst.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.dccount.p, plan.ccount.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.dhfirst.p, plan.hv_first.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(W.dhcount.p, plan.hv_count.data(), nsec * sizeof(int), cudaMemcpyHostToDevice, st);
+    // the host vectors above are freed on return: the uploads must have finished
+    if (cudaStreamSynchronize(st) != cudaSuccess) return set_error(ED_ERR_CUDA, "ed_batch_lanczos: table upload");
+    return ED_OK;
+}
+
+// The m steps of the recursion on stream `st` (recorded into the graph when `st` is capturing).
+// Per step: the fused H.v of every kind, the per-sector scalars and the update; the exact-norm
+// launches return at once unless a sector's step flagged cancellation.
+template <typename R, bool CPLX>
+static int batch_steps(BatchWorkspace& W, const Sector& s0, const HvWeights& w, cudaStream_t st) {
+    uint8_t* b[2] = {W.buf0.p, W.buf1.p};
+    for (int k = 0; k < W.m; ++k) {
         void* v = b[k % 2];
         void* other = b[(k + 1) % 2];
-        StepArgs a{dviews.p, doffs.p, dhv.p, dkidx.p, 0, 0, smem, w, v, other, other, k == 0, coef, stride, k,
-                    partials.p, dtasks.p, ntasks, (int64_t)s0.n_spin, xfull.p};
-        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid, s0.cand_grid_f32,
-                                 plan.kind_first, plan.kind_count, a, cap)) {
-            if (use_graph) {
-                cudaGraph_t g = nullptr;
-                cudaStreamEndCapture(cap, &g);
-                if (g) cudaGraphDestroy(g);
-                cudaStreamDestroy(priv);
+        StepArgs a{W.dviews.p, W.doffs.p, W.dhv.p, W.dkidx.p, 0, 0, W.smem, w, v, other, other, k == 0, W.coef.p,
+                   W.stride, k, W.partials.p, W.dtasks.p, W.ntasks, (int64_t)s0.n_spin, W.xfull.p};
+        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.hv_grid, s0.other_grid,
+                                 s0.cand_grid_f32, W.kind_first, W.kind_count, a, st))
+            return rc;
+        lanczos_scalars_kernel<<<W.nsec, kScalarThreads, 0, st>>>(W.partials.p, W.dhfirst.p, W.dhcount.p, W.coef.p,
+                                                                  W.stride, k, 0, 0);
+        lanczos_update_kernel<R, CPLX><<<W.grid, kUpdThreads, 0, st>>>(W.doffs.p, W.dchunks.p, W.nchunks, v, other,
+                                                                       W.coef.p, W.stride, k, 0, 0);
+        // sectors whose b needs the exact norm: y - a v and its norm, b, then v_{k+1} /= b
+        lanczos_exact_kernel<R, CPLX><<<W.grid, kUpdThreads, 0, st>>>(W.doffs.p, W.dchunks.p, W.dcfirst.p,
+                                                                      W.dccount.p, W.nsec, v, other, W.coef.p,
+                                                                      W.stride, k, W.partials.p);
+        lanczos_scalars_kernel<<<W.nsec, kScalarThreads, 0, st>>>(W.partials.p, W.dcfirst.p, W.dccount.p, W.coef.p,
+                                                                  W.stride, k, 2, 0);
+        lanczos_scale_kernel<R, CPLX><<<W.grid, kUpdThreads, 0, st>>>(W.doffs.p, W.dchunks.p, W.dcfirst.p,
+                                                                      W.dccount.p, W.nsec, other, W.coef.p, W.stride, k);
+    }
+    return ED_OK;
+}
+
+template <typename R, bool CPLX>
+static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& w, const void* const* v0, int m,
+                       double* coef, int use_graph, cudaStream_t st) {
+    std::lock_guard<std::mutex> lock(g_batch_mu);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int dtype = dtype_code(sizeof(R) == 8, CPLX);
+    const Sector& s0 = *secs[0];
+    if (!g_batch || !g_batch->matches(secs, dev, dtype, m, w, use_graph)) {
+        drop_batch_workspace();  // the old workspace's memory first
+        auto* W = new (std::nothrow) BatchWorkspace();
+        if (!W) return set_error(ED_ERR_NOMEM, "ed_batch_lanczos: host allocation");
+        W->device = dev;
+        W->dtype = dtype;
+        W->m = m;
+        W->use_graph = use_graph;
+        W->w = w;
+        W->minb = s0.hv_minb;
+        W->hv_grid = s0.hv_grid;
+        W->other_grid = s0.other_grid;
+        W->cand_grid = s0.cand_grid_f32;
+        for (const Sector* s : secs) W->serials.push_back(s->serial);
+        int rc = batch_prepare<R, CPLX>(*W, secs, m, st);
+        if (rc == ED_OK && use_graph) {
+            // capture the m steps once on a private stream; later calls of this shape replay them
+            cudaGraph_t graph = nullptr;
+            if (cudaStreamCreateWithFlags(&W->priv, cudaStreamNonBlocking) != cudaSuccess)
+                rc = set_error(ED_ERR_CUDA, "ed_batch_lanczos: stream");
+            else if (cudaStreamBeginCapture(W->priv, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                rc = set_error(ED_ERR_CUDA, "ed_batch_lanczos: begin capture");
+            else {
+                rc = batch_steps<R, CPLX>(*W, s0, w, W->priv);
+                cudaError_t e = cudaStreamEndCapture(W->priv, &graph);
+                if (rc == ED_OK && e == cudaSuccess) e = cudaGraphInstantiate(&W->exec, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
+                if (rc == ED_OK && e != cudaSuccess) rc = set_cuda_error(e, "ed_batch_lanczos: graph");
             }
+        }
+        if (rc != ED_OK) {
+            delete W;
             return rc;
         }
-        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dhfirst.p, dhcount.p, coef, stride, k, 0, 0);
-        lanczos_update_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, nchunks, v, other, coef,
-                                                                      stride, k, 0, 0);
-        // sectors whose b needs the exact norm: y - a v and its norm, b, then v_{k+1} /= b
-        lanczos_exact_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, dcfirst.p, dccount.p, nsec,
-                                                                     v, other, coef, stride, k, partials.p);
-        lanczos_scalars_kernel<<<nsec, kScalarThreads, 0, cap>>>(partials.p, dcfirst.p, dccount.p, coef, stride, k, 2,
-                                                                 0);
-        lanczos_scale_kernel<R, CPLX><<<grid, kUpdThreads, 0, cap>>>(doffs.p, dchunks.p, dcfirst.p, dccount.p, nsec,
-                                                                     other, coef, stride, k);
+        g_batch = W;
     }
+    BatchWorkspace& W = *g_batch;
+    const size_t esz = sizeof(typename Vec<R, CPLX>::T);
+    cudaMemsetAsync(W.coef.p, 0, (size_t)W.nsec * W.stride * sizeof(double), st);
+    for (int s = 0; s < W.nsec; ++s)
+        if (W.hn[s]) cudaMemcpyAsync(W.buf0.p + W.hoffs[s] * esz, v0[s], W.hn[s] * esz, cudaMemcpyDeviceToDevice, st);
+    // start vectors: |v0| and normalisation
+    norm_partials_kernel<R, CPLX><<<W.grid, 256, 0, st>>>(W.doffs.p, W.dchunks.p, W.nchunks, W.buf0.p, W.partials.p);
+    lanczos_scalars_kernel<<<W.nsec, kScalarThreads, 0, st>>>(W.partials.p, W.dcfirst.p, W.dccount.p, W.coef.p,
+                                                              W.stride, 0, 1, W.stride - 1);
+    lanczos_update_kernel<R, CPLX><<<W.grid, kUpdThreads, 0, st>>>(W.doffs.p, W.dchunks.p, W.nchunks, W.buf0.p,
+                                                                   nullptr, W.coef.p, W.stride, 0, 1, W.stride - 1);
+    ED_CHECK_LAUNCH("batch start vectors");
     if (use_graph) {
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        cudaError_t e = cudaStreamEndCapture(cap, &graph);
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-        if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        cudaStreamDestroy(priv);
-        if (e != cudaSuccess) return set_cuda_error(e, "ed_batch_lanczos: graph");
+        const cudaError_t e = cudaGraphLaunch(W.exec, st);
+        if (e != cudaSuccess) return set_cuda_error(e, "ed_batch_lanczos: graph launch");
     } else {
+        if (int rc = batch_steps<R, CPLX>(W, s0, w, st)) return rc;
         ED_CHECK_LAUNCH("batch steps");
-        if (cudaStreamSynchronize(st) != cudaSuccess) return set_error(ED_ERR_CUDA, "ed_batch_lanczos: steps");
     }
+    cudaMemcpyAsync(coef, W.coef.p, (size_t)W.nsec * W.stride * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_cuda_error(e, "ed_batch_lanczos: steps");
     return ED_OK;
 }
 

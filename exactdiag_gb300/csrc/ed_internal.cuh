@@ -125,6 +125,7 @@ struct ChunkPlan {
 
 struct Sector {
     SectorView view{};
+    uint64_t serial = 0;         // unique per created sector in this process (batch workspace key)
     int64_t n_hole_masks = 0;
     uint64_t n_spin = 0;
     int kx_raw = 0;
@@ -277,6 +278,7 @@ int corr_launch(const Sector& s, int dtype, const void* psi, int kind, int nfixe
                 cudaStream_t st);
 int excite_launch(const Sector& src, const Sector& dst, int op, int qx, int qy, int initial_sz2, int dtype,
                   const void* x, void* y, cudaStream_t st);
+void batch_forget(const Sector& s);  // frees the kept batch workspace if it holds s
 int batch_lanczos_launch(const std::vector<const Sector*>& secs, const HvWeights& w, int dtype, const void* const* v0,
                          int m, double* coef, int use_graph, cudaStream_t st);
 int project_launch(const Sector& s, int dtype, const void* V, int k, void* w, double* coef, double* scratch,

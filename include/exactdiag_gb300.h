@@ -47,6 +47,7 @@ typedef struct ed_sector ed_sector;
  * State_Index_Amplitude_Translator (symmetry_ladder.h:271-406) and
  * Symmetries_Single_Spin_Half_2leg_Ladder (symmetry_ladder.h:55-269). */
 int ed_sector_create(int L, int Nh, int Nd, int kx, int ky, ed_sector** out);
+/* Frees the sector (and the kept ed_batch_lanczos workspace when it holds this sector). */
 int ed_sector_destroy(ed_sector* s);
 
 /* Enumerates the representatives on the device.  Replaces get_basis_map /
@@ -68,6 +69,11 @@ int ed_sector_row_kinds(const ed_sector* sector, int counts[3]);
 
 /* Rows of the sector per row kind, in the order of ed_sector_row_kinds. */
 int ed_sector_kind_rows(const ed_sector* sector, int64_t rows[3]);
+
+/* Kernel launches of one ed_lanczos_step on this sector: the expanded copies (when the sector has
+ * any), one fused H.v kernel per row kind present, the scalar reduction and the four launches of the
+ * update.  No reference counterpart (a property of this engine's step). */
+int ed_sector_step_launches(const ed_sector* sector, int* launches);
 
 /* Number of representatives (Basis_Index_Map::get_num_states, basis_indexing.h:180-182). */
 int ed_basis_size(const ed_sector* s, int64_t* n);
@@ -184,6 +190,11 @@ int ed_singlet_correlations(const ed_sector* sector, int dtype, const void* psi_
  * sectors must share L, Nh and Nd.  coef_dev holds nsec * (2m+4) doubles
  * (device); sector s's block X: X[2k+1] = a_k, X[2k+2] = b_{k+1}, X[2m+3] = |v0|.
  * The caller truncates after the first b_{k+1} < 1e-8.  Synchronises `stream`.
+ * The workspace (two vectors per sector, chunk tables, scratch) and the captured
+ * graph are kept after the call for the next call with the same sectors in the
+ * same order, dtype, m, weights, use_graph and launch shape; one such workspace
+ * is kept per process, replaced by a call of another shape and freed when one of
+ * its sectors is destroyed.  Calls are serialised by a lock.
  * Replaces the per-q loop of tJ_spin_half_ladder/api.py:116-161 over
  * general/lanczos_diagonalization.py:124-175. */
 int ed_batch_lanczos(const ed_sector* const* sectors, int nsec, const double weights[4], int dtype,

@@ -35,6 +35,7 @@
 #include "general/basis_indexing.h"
 #include "general/column_functions.h"
 #undef pop_back
+#include "general/cpp_sparse_dot.h"
 
 namespace {
 
@@ -375,6 +376,23 @@ int ref_basis_load(const char* path, int64_t* out_sparse, int32_t* out_orbit, in
     } catch (...) {
         return -1;
     }
+}
+
+// general/cython_sparse_dot.pyx:40-80, the row-major Hermitian-triangle branch of sparse_matrix_dot at
+// num_threads = 1 (one explicit-pass call per row, then one conjugate pass over the whole column
+// range), calling the reference's own cpp_sparse_dot.h:59-71 and :104-138.  vals/x/y are complex128
+// as interleaved doubles; y accumulates (first_set_to_zero = False).
+int ref_sparse_matrix_dot_row_major(int64_t n, const int64_t* row_ptr, const int64_t* cols, const int16_t* vidx,
+                                    const double* vals, const double* x, double* y, double w_re, double w_im) {
+    const auto* v = reinterpret_cast<const complex<double>*>(vals);
+    const auto* xi = reinterpret_cast<const complex<double>*>(x);
+    auto* yo = reinterpret_cast<complex<double>*>(y);
+    const complex<double> w(w_re, w_im);
+    const auto* rp = reinterpret_cast<const long long*>(row_ptr);
+    const auto* ci = reinterpret_cast<const long long*>(cols);
+    for (long long r = 0; r < n; ++r) yo[r] += w * matvec_explicit_elements_pass_row_major(r, rp, v, vidx, ci, xi);
+    matvec_hermitian_conjugate_pass_row_major(0, n, n, rp, v, vidx, ci, xi, true, yo, w);
+    return 0;
 }
 
 }  // extern "C"

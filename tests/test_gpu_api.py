@@ -235,6 +235,29 @@ def test_batch_lanczos_matches_single(torch):
             assert np.array_equal(a, a1) and np.array_equal(b, b1) and nrm == n1
 
 
+def test_batch_workspace_reuse(torch):
+    """A second call of the same batch shape replays the kept graph on new start vectors; a call of
+    another shape (different m, then a sector destroyed) rebuilds it.  Every result equals the
+    single-sector recursion bit for bit."""
+    from exactdiag_gb300.engine import batch_lanczos
+    from exactdiag_gb300.lanczos import lanczos_coefficients
+
+    secs = [_sector((6, 2, 5, kx, 0)) for kx in range(3)]
+
+    def check(v0s, m):
+        outs = batch_lanczos(secs, W, v0s, m)
+        for s, v, (a, b, nrm) in zip(secs, v0s, outs):
+            a1, b1, n1 = lanczos_coefficients(s, W, v.clone(), m)
+            assert np.array_equal(a, a1) and np.array_equal(b, b1) and nrm == n1
+
+    for seed in (40, 41):
+        check([torch.as_tensor(seeded_vector(s.n, seed + i, True), device=s.device) for i, s in enumerate(secs)], 20)
+    check([torch.as_tensor(seeded_vector(s.n, 50 + i, True), device=s.device) for i, s in enumerate(secs)], 17)
+    secs[1].close()
+    secs[1] = _sector((6, 2, 5, 1, 0))
+    check([torch.as_tensor(seeded_vector(s.n, 60 + i, True), device=s.device) for i, s in enumerate(secs)], 17)
+
+
 def _spectrum_config(L, Nh, name, broadening=0.05, omega_min=0.0, omega_max=6.0, steps=300, m=60):
     from exactdiag_gb300.tJ_spin_half_ladder import configs
 

@@ -26,7 +26,7 @@ def _worker(rank, world, port, queue):
     import bench
 
     local = [10.0 + 5.0 * rank, 20.0 - 3.0 * rank]  # per-step ms of (mixed, fp64) on this replica
-    ms, value = bench.aggregate_replicas(local, steps=7, world=world, device="cpu")
+    ms, value = bench.aggregate_replicas(local, world=world, device="cpu")
     dist.barrier()
     queue.put((rank, ms, value))
     dist.destroy_process_group()
@@ -51,5 +51,5 @@ def test_replica_aggregation_world2():
 def test_single_rank_needs_no_process_group():
     import bench
 
-    ms, value = bench.aggregate_replicas([4.0, 8.0], steps=3, world=1)
+    ms, value = bench.aggregate_replicas([4.0, 8.0], world=1)
     assert ms == [4.0, 8.0] and value == pytest.approx(250.0)

@@ -656,11 +656,20 @@ def cpu_baseline(args) -> dict:
 
 
 def _throughput_child(ref: CpuReference, K: int, W: int, barrier, conn) -> None:
+    """W + K sample steps in lock step with the other processes: every process flushes its cache,
+    then all start the timed part together, and none flushes again before all have finished it (so
+    the flushes never overlap another process's timed work)."""
     ref.own_output()
-    for _ in range(W):
-        ref.step()
-    barrier.wait()
-    conn.send([ref.step() for _ in range(K)])
+    out = []
+    for k in range(W + K):
+        ref.flush_cache()
+        barrier.wait()
+        ts = ref.spmv_seconds()
+        tv = ref.vec_seconds()
+        barrier.wait()
+        if k >= W:
+            out.append((ts + tv, ts * ref.n / len(ref.rows) + tv * ref.n / ref.vec_sample))
+    conn.send(out)
     conn.close()
 
 
@@ -697,10 +706,14 @@ def run_reference(args, rank: int) -> dict | None:
         p.start()
         pipes.append(a)
         children.append(p)
-    barrier.wait()
-    t0 = time.perf_counter()
-    results = [a.recv() for a in pipes]
+    # the parent keeps step with the children (two barriers per step) and times the K timed steps
+    for k in range(W + K):
+        if k == W:
+            t0 = time.perf_counter()
+        barrier.wait()
+        barrier.wait()
     wall = time.perf_counter() - t0
+    results = [a.recv() for a in pipes]
     for p in children:
         p.join()
     child_full = [float(np.mean([s[1] for s in r])) for r in results]
@@ -713,8 +726,8 @@ def run_reference(args, rank: int) -> dict | None:
         "config": bench_config(ref.n),
         "precision": "complex128 (the reference's value type)",
         "timing": {
-            "ms_per_step_is": "wall time of one sample step of the throughput run (all processes at once); "
-                              "K of them are the timed region",
+            "ms_per_step_is": "wall time of one sample step of the throughput run (all processes at once, "
+                              "each flushing its cache before the step); K of them are the timed region",
             "value_is": f"sum over {procs} processes of 1 / (their mean full-step time, each sample step scaled "
                         "by n/sample)",
             "full_step_s_throughput_mean": float(np.mean(child_full)),

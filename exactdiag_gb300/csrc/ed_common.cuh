@@ -136,13 +136,15 @@ struct SegHopDesc {
 
 // Per segment of a free block, a record of rec_len 32-bit words (built once per sector by
 // seg_records_kernel; the values depend on the segment's high part only, never on a vector):
-//   [0] the segment's first row in the block;  [1] zbr | zbl << 8 | hib << 16;
-//   [2, 2 + RB) the first rows of the partner segments of its zbr antiparallel high rung bonds, then
-//   the segment's own first row up to a multiple of four; [2 + RB, 2 + RB + LB) the same for its zbl
-//   leg bonds; [xo, xo + nX) cross bond c: first row of the partner segment; hop h from word
-//   hop_off[h]: the first n0 hops (nb = 0, and absent hops) the target's high-part rank; the next n12
-//   (nb 1 or 2) ua, then the 2^nb high-part ranks by vbi; the rest (nb = 3) pi(H << P); then two zero
-//   words (zero_w), which the kernel's padding hops read.
+//   [0] the segment's first row in the block;  [1] zb | zbr << 8 | hib << 16 (antiparallel high
+//   bonds, the rung bonds among them, the spins at the high ends of the cross bonds); [2, 4) zero;
+//   [4, 4 + zb) the first rows of the partner segments of its antiparallel high bonds, rung bonds
+//   first, then the segment's own first row up to a multiple of four (HB words are reserved; the
+//   list starts on a 16-byte boundary and is read four words at a time);
+//   [xo, xo + nX) cross bond c: first row of the partner segment; hop h from word hop_off[h]: the
+//   first n0 hops (nb = 0, and absent hops) the target's high-part rank; the next n12 (nb 1 or 2) ua,
+//   then the 2^nb high-part ranks by vbi; the rest (nb = 3) pi(H << P); then two zero words
+//   (zero_w), which the kernel's padding hops read.
 struct alignas(16) SegDesc {
     int64_t start;              // the block's first row
     int64_t rec;                // first word of the block's segment records
@@ -151,7 +153,7 @@ struct alignas(16) SegDesc {
     uint8_t cX[kSegMaxX][2];    // bonds across P: (end below P, end at or above P), rung bonds first
     uint32_t mr, ma, m2;        // lower ends of the rung / leg-1 / leg-2 bonds at or above P
     uint8_t nA, nAr, nB, nBr, nBa, nX, nXr, nhop;
-    uint8_t ok, RB, LB, xo;     // ok: every term fits the limits; record layout (above)
+    uint8_t ok, HB, xo, pad1;   // ok: every term fits the limits; record layout (above)
     uint32_t rec_len;           // words per segment record, a multiple of 4
     uint8_t hop_off[kMaxHops];  // first word of hop h in a record
     uint8_t n0, n12, zero_w, pad2;  // hops by kind (record layout above); two zero words from zero_w

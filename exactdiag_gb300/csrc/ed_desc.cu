@@ -204,11 +204,10 @@ SegDesc make_seg_desc(const BlockDesc& D, int Ns, int P, const std::vector<int>&
             }
         for (int t = 0; t < D.nhop; ++t) G.hop[t] = sorted[t];
     }
-    // record layout: header, high-bond partners (rung, leg; each padded to a multiple of four), cross
+    // record layout: header, high-bond partners (rung then leg, padded to a multiple of four), cross
     // partners, then each hop's words
-    G.RB = (uint8_t)((G.nBr + 3) & ~3);
-    G.LB = (uint8_t)((G.nB - G.nBr + 3) & ~3);
-    uint32_t w = 2u + G.RB + G.LB;
+    G.HB = (uint8_t)((G.nB + 3) & ~3);
+    uint32_t w = 4u + G.HB;
     G.xo = (uint8_t)w;
     w += G.nX;
     for (int t = 0; t < D.nhop; ++t) {

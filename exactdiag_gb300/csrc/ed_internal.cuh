@@ -72,6 +72,7 @@ constexpr int kChunkRows = 8192;
 // chunk of it holds.
 constexpr int kSegThreads = 256;
 constexpr int kSegChunkRows = 16384;
+constexpr int kSegWin = 64;  // offsets of a segment one warp covers in a segment chunk (two rows per lane)
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
 enum RowKind : int {
@@ -94,7 +95,7 @@ struct BatchChunk {
     int64_t xoff;        // stabiliser blocks: first element of the block's expanded copy (ExpandTask);
                          // segment chunks: first element of the sector's copies; else -1
     int32_t kl;          // segment chunks (free blocks, ed_seg.cuh): down spins below P; row chunks: -1
-    int32_t piece;       // segment chunks of more than 16 rows per segment: rows [32 piece, 32 piece + 32)
+    int32_t piece;       // segment chunks: the window of offsets [kSegWin piece, kSegWin piece + kSegWin)
 };
 
 // One stabiliser block of a step layout whose vector entries are expanded, every step, to all

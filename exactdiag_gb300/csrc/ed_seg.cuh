@@ -157,7 +157,43 @@ __device__ __forceinline__ void seg_cp_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <typename R, bool CPLX, int MINB>
+// Adds a partner's value to a row's exchange sum: the one sum when rung and leg J agree, else the
+// rung or the leg sum.
+template <typename R, bool CPLX, bool MERGED>
+__device__ __forceinline__ void seg_add(R& er, R& ei, R& lr, R& li, bool rung, R vr, R vi) {
+    if (MERGED || rung) {
+        er += vr;
+        if constexpr (CPLX) ei += vi;
+    } else {
+        lr += vr;
+        if constexpr (CPLX) li += vi;
+    }
+}
+
+constexpr int kSegLowMax = 16;  // antiparallel bonds below P of one row (at most kSegMaxA), padded to fours
+
+// A hop slot of a chunk as every row reads it: the target values, the coefficient, the slot's first
+// record word.  Staged in shared memory; one 16-byte load for real FP32 vectors.
+template <typename R, bool CPLX>
+struct alignas(16) SegSlot {
+    const typename Vec<R, CPLX>::T* tp;
+    R cr;
+    uint32_t off;
+};
+template <typename R>
+struct alignas(16) SegSlot<R, true> {
+    const typename Vec<R, true>::T* tp;
+    R cr, ci;
+    uint32_t off;
+};
+
+// The fused step over segment chunks: a chunk is (free block, class kl, 64-offset window, range of
+// segments); warp w of the CTA takes segments begin + w, begin + w + 8, ... and, in each, the rows at
+// offsets t = window + lane and t + 32.  NR rows are worked on together (their gathers in flight
+// at once, the segment's record words read once for both); NR = 1 takes the two rows one after
+// the other.  MERGED: rung and leg exchanges share one coefficient (J_rung = J_leg), so each row keeps
+// one exchange sum over one list per bond class; otherwise every element picks its coefficient.
+template <typename R, bool CPLX, int MINB, bool MERGED, int NR>
 __global__ void __launch_bounds__(kSegThreads, MINB)
     seg_step_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                     const BatchChunk* __restrict__ chunks, const int* __restrict__ idx, int count, HvWeights W,
@@ -171,18 +207,17 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     __shared__ __align__(16) SegDesc s_desc;
     __shared__ __align__(16) SegHop<R, CPLX> s_hop[kMaxHops];
     // hop slots of the chunk: the kind-0 hops then dummies up to a multiple of four, the same for kind 1
-    // (nb 1 or 2); a dummy reads the first element of the block with coefficient 0
-    __shared__ const T* s_stp[kSegHopSlots];
-    __shared__ R s_scr[kSegHopSlots], s_sci[kSegHopSlots];
-    __shared__ uint32_t s_soff[kSegHopSlots];
-    // per-lane terms of the chunk (every warp maps its lanes to the same offsets t)
-    __shared__ uint8_t s_ar[8][32];             // rank_P of the rung-bond partners below P, padded with t
-    __shared__ uint8_t s_al[16][32];            // the same for leg bonds
-    __shared__ uint8_t s_xo[kSegMaxX][32];      // cross bond c: rank_P(Lo ^ low end) (0 past nX)
-    __shared__ uint16_t s_hc[kSegHopSlots][32]; // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA (kind 1)
-    __shared__ uint32_t s_lane[32];             // Lo | lob << 16 (cross-bond low-end spins)
-    __shared__ uint32_t s_cnt[32];              // nr | nl << 8 (antiparallel low bonds by kind)
-    __shared__ int s_max[2];                    // the chunk's longest rung and leg lists, in fours
+    // (nb 1 or 2); a dummy reads the block's first element with coefficient 0
+    __shared__ __align__(16) SegSlot<R, CPLX> s_slot[kSegHopSlots];
+    // per-offset terms of the chunk's window (column j = offset - window; every warp maps its lanes to
+    // the same columns): a column past the class's rows repeats column j - 32, so its reads stay valid
+    __shared__ uint8_t s_al[kSegLowMax][kSegWin];      // partners of the antiparallel bonds below P (rung
+                                                       // first), padded with the offset itself
+    __shared__ uint8_t s_xo[kSegMaxX][kSegWin];        // cross bond c: rank_P(Lo ^ low end) (0 past nX)
+    __shared__ uint16_t s_hc[kSegHopSlots][kSegWin];   // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA
+    __shared__ uint32_t s_lane[kSegWin];               // Lo | lob << 16 (cross-bond low-end spins)
+    __shared__ uint32_t s_cnt[kSegWin];                // nr | nlow << 8 (antiparallel bonds below P)
+    __shared__ int s_maxw[2];                          // longest low list of each half, in fours
     __shared__ __align__(16) uint32_t s_rec[kWarps][2][kSegRecMax];  // per warp: this and the next record
     const int P = views[0].seg_p;
     const uint32_t amask = (1u << P) - 1u;
@@ -215,9 +250,8 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int kl = ch.kl, Ns = Sp->Ns, Nd = Sp->Nd, N = Sp->N, L = Sp->L;
         const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
         const int nA = (int)comb[kl * kCombStride + P];
-        const int t = 32 * ch.piece + lane;   // a warp takes one 32-row piece of a segment
-        const int nact = min(32, nA - 32 * ch.piece);
-        const bool act = lane < nact;
+        const int win = kSegWin * ch.piece;
+        const int nact = min(32, nA - win);  // lanes with a first row
         __syncthreads();  // the previous chunk's rows are done with the shared tables
         {
             const uint4* src = reinterpret_cast<const uint4*>(Sp->seg + ch.block);
@@ -229,10 +263,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int64_t bstart = s_desc.start;
         T* const x = reinterpret_cast<T*>(v) + offs[ch.sec];
         const T* const xb = x + bstart;
-        if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + kMaxHops) {
-            // every hop slot gets a record: absent hops (and slots past nhop) read a valid element with
+        if (warp == 2 && lane < kMaxHops) {
+            // every hop gets a record: absent hops (and those past nhop) read a valid element with
             // coefficient 0
-            const int h = threadIdx.x - 32;
+            const int h = lane;
             SegHop<R, CPLX>& F = s_hop[h];
             const SegHopDesc& G = s_desc.hop[h];
             const bool live = h < nhop && G.kind != 3 && W.w[G.term] != 0.0;
@@ -272,75 +306,80 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
             }
         }
-        if (warp == 0) {
-            // the per-lane tables; the partner lists are padded with the row's own offset to their full
-            // length (the padding is read in groups of four and taken back out after the sums)
-            const uint32_t lo = act ? s_ut[s_utoff[kl] + t] : 0u;
-            const uint8_t tt = (uint8_t)(act ? t : 0);
-            int nr = 0, nl = 0;
+        // the offset whose terms column j holds: its own, or (past the class's rows) column j - 32's
+        const int jcol = 32 * warp + lane;  // warps 0 and 1
+        int tsrc = win + jcol;
+        if (warp < 2 && tsrc >= nA) tsrc = (win + lane < nA) ? win + lane : win;
+        const uint32_t lo_c = (warp < 2 && tsrc < nA) ? s_ut[s_utoff[kl] + tsrc] : 0u;
+        if (warp < 2) {
+            // bonds below P: the antiparallel ones' partners, rung bonds first, padded with the offset
+            // itself up to the table's length (read in fours, the padding taken back out after the sums)
+            int nr = 0, nlow = 0;
             const int nAb = s_desc.nA, nAr = s_desc.nAr;
-            for (int i = 0; i < nAb && act; ++i) {
-                const uint32_t f = s_desc.fA[i], sb = lo & f;
+            for (int i = 0; i < nAb; ++i) {
+                const uint32_t f = s_desc.fA[i], sb = lo_c & f;
                 if (sb != 0u && sb != f) {
-                    if (i < nAr) s_ar[nr++][lane] = s_rt[lo ^ f];
-                    else s_al[nl++][lane] = s_rt[lo ^ f];
+                    s_al[nlow++][jcol] = s_rt[lo_c ^ f];
+                    if (i < nAr) ++nr;
                 }
             }
-            const int mr = (int)__reduce_max_sync(0xffffffffu, (unsigned)nr);
-            const int ml = (int)__reduce_max_sync(0xffffffffu, (unsigned)nl);
-            for (int q = nr; q < 8; ++q) s_ar[q][lane] = tt;
-            for (int q = nl; q < 16; ++q) s_al[q][lane] = tt;
+            for (int q = nlow; q < kSegLowMax; ++q) s_al[q][jcol] = (uint8_t)tsrc;
+            const int mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow);
             uint32_t lob = 0;
             for (int cc = 0; cc < kSegMaxX; ++cc) {
                 const uint32_t a = s_desc.cX[cc][0];
-                if (cc < nX) lob |= ((lo >> a) & 1u) << cc;
-                s_xo[cc][lane] = act && cc < nX ? s_rt[lo ^ (1u << a)] : (uint8_t)0;
+                if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
+                s_xo[cc][jcol] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
             }
-            s_lane[lane] = lo | (lob << 16);
-            s_cnt[lane] = (uint32_t)nr | ((uint32_t)nl << 8);
-            if (lane == 0) {
-                s_max[0] = (mr + 3) & ~3;
-                s_max[1] = (ml + 3) & ~3;
-            }
+            s_lane[jcol] = lo_c | (lob << 16);
+            s_cnt[jcol] = (uint32_t)nr | ((uint32_t)nlow << 8);
+            if (lane == 0) s_maxw[warp] = (mx + 3) & ~3;
         }
         __syncthreads();
         const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
-        if (warp == 0) {
-            const uint32_t lo = s_lane[lane] & 0xffffu;
+        if (warp < 2) {
             for (int sl = 0; sl < n04 + n124; ++sl) {
                 const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
                 uint32_t hc = 0;
-                if (act && h >= 0 && s_hop[h].kind != 3) {
+                if (h >= 0 && s_hop[h].kind != 3) {
                     const SegHop<R, CPLX>& F = s_hop[h];
-                    const uint32_t V = seg_perm(lo, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
+                    const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
                     hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
                 }
-                s_hc[sl][lane] = (uint16_t)hc;
+                s_hc[sl][jcol] = (uint16_t)hc;
             }
-        } else if (warp == 1 && lane < n04 + n124) {
+        } else if (warp == 2 && lane < n04 + n124) {
             const int sl = lane;
             const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
-            s_stp[sl] = h >= 0 ? s_hop[h].tp : xb;
-            s_scr[sl] = h >= 0 ? s_hop[h].cr : R(0);
-            s_sci[sl] = h >= 0 ? s_hop[h].ci : R(0);
-            s_soff[sl] = h >= 0 ? s_desc.hop_off[h] : s_desc.zero_w;
+            SegSlot<R, CPLX>& S = s_slot[sl];
+            S.tp = h >= 0 ? s_hop[h].tp : xb;
+            S.cr = h >= 0 ? s_hop[h].cr : R(0);
+            if constexpr (CPLX) S.ci = h >= 0 ? s_hop[h].ci : R(0);
+            S.off = h >= 0 ? s_desc.hop_off[h] : s_desc.zero_w;
         }
         __syncthreads();
 
-        const int mr4 = s_max[0], ml4 = s_max[1];  // list lengths read, rounded up to groups of four
-        const uint32_t cnt = s_cnt[lane], ln = s_lane[lane];
-        const int nr = (int)(cnt & 255u), nl = (int)(cnt >> 8);
-        const uint32_t lo = ln & 0xffffu, lob = ln >> 16;
-        const int pad_r = mr4 - nr, pad_l = ml4 - nl;
-        const uint32_t rec_len = s_desc.rec_len, RB = s_desc.RB, xo = s_desc.xo;
+        const int smax = max(s_maxw[0], s_maxw[1]);  // low lists read, in fours
+        const uint32_t rec_len = s_desc.rec_len, xo = s_desc.xo;
         const uint32_t* __restrict__ rec0 = Sp->seg_rec + s_desc.rec + (int64_t)Sp->seg_off[kl] * rec_len;
         const uint32_t* __restrict__ segb = Sp->seg_base + Sp->seg_off[kl];
         const int nX4 = (nX + 3) & ~3;  // cross bonds read in groups of four (the padding is never antiparallel)
-        const uint32_t xall = (1u << nX) - 1u, xrmask = (1u << nXr) - 1u, xlmask = ((1u << nX4) - 1u) & ~xrmask;
+        const uint32_t xall = (1u << nX) - 1u, xrmask = (1u << nXr) - 1u, x4mask = (1u << nX4) - 1u;
         T* const y = reinterpret_cast<T*>(other) + offs[ch.sec] + bstart;
         const T* const yp = first ? nullptr : reinterpret_cast<const T*>(vprev) + offs[ch.sec] + bstart;
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
-        const T* const xt = xb + t;  // this row's offset in every segment of the block
+        // per half h of the window: this lane's offset, whether it is a row, the offset read for it
+        int tt[2];
+        bool act[2];
+        uint32_t lnw[2], cnt[2];  // s_lane and s_cnt of the two columns (fields unpacked where used)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int t = win + lane + 32 * h;
+            act[h] = t < nA;
+            tt[h] = act[h] ? t : win + lane;
+            lnw[h] = s_lane[lane + 32 * h];
+            cnt[h] = s_cnt[lane + 32 * h];
+        }
         uint32_t* const srec0 = s_rec[warp][0];
         uint32_t* const srec1 = s_rec[warp][1];
 
@@ -348,179 +387,224 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         R pend[kReduceSlots] = {R(0), R(0), R(0), R(0)};
         int npend = 0;
 
-        // the next segment's record is copied into shared memory, and its row value and v_{k-1} loaded,
-        // while this one is worked on; the piece's active lanes together copy every word of a record
-        int64_t g = act ? ch.begin + warp : ch.end;  // lanes past the piece's rows skip to the reduction
-        if (g < ch.end)
+        // the next segment's record is copied into shared memory, and its rows' values and v_{k-1}
+        // loaded, while this one is worked on; the active lanes together copy every word of a record
+        // segment indices of a class fit 32 bits (SectorView::seg_off)
+        const int gend = (int)ch.end;
+        int g = lane < nact ? (int)ch.begin + warp : gend;  // lanes without a row skip to the reduction
+        if (g < gend)
             for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
-                seg_cp_async16(srec0 + w4, rec0 + g * (int64_t)rec_len + w4);
+                seg_cp_async16(srec0 + w4, rec0 + (uint32_t)g * rec_len + w4);
         seg_cp_commit();
         uint32_t base = 0;
-        R xr = R(0), xi = R(0), pr = R(0), pi = R(0);
-        if (g < ch.end) {
+        R xr[2] = {R(0), R(0)}, xi[2] = {R(0), R(0)}, pr[2] = {R(0), R(0)}, pi[2] = {R(0), R(0)};
+        if (g < gend) {
             base = __ldg(segb + g);
-            seg_ld<R, CPLX>(xt + base, xr, xi);
-            if (!first) seg_ld<R, CPLX>(yp + base + t, pr, pi);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                seg_ld<R, CPLX>(xb + base + tt[h], xr[h], xi[h]);
+                if (!first) seg_ld<R, CPLX>(yp + base + tt[h], pr[h], pi[h]);
+            }
         }
-        for (int it = 0; g < ch.end; ++it, g += kWarps) {
+        for (int it = 0; g < gend; ++it, g += kWarps) {
             const uint32_t* const sw = (it & 1) ? srec1 : srec0;
-            const int64_t gn = g + kWarps;
-            if (gn < ch.end) {
+            const int gn = g + kWarps;
+            if (gn < gend) {
                 uint32_t* const dst = (it & 1) ? srec0 : srec1;
                 for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
-                    seg_cp_async16(dst + w4, rec0 + gn * (int64_t)rec_len + w4);
+                    seg_cp_async16(dst + w4, rec0 + (uint32_t)gn * rec_len + w4);
             }
             seg_cp_commit();
             uint32_t nbase = 0;
-            R nxr = R(0), nxi = R(0), npr = R(0), npi = R(0);
-            if (gn < ch.end) {
+            R nxr[2] = {R(0), R(0)}, nxi[2] = {R(0), R(0)}, npr[2] = {R(0), R(0)}, npi[2] = {R(0), R(0)};
+            if (gn < gend) {
                 nbase = __ldg(segb + gn);
-                seg_ld<R, CPLX>(xt + nbase, nxr, nxi);
-                if (!first) seg_ld<R, CPLX>(yp + nbase + t, npr, npi);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    seg_ld<R, CPLX>(xb + nbase + tt[h], nxr[h], nxi[h]);
+                    if (!first) seg_ld<R, CPLX>(yp + nbase + tt[h], npr[h], npi[h]);
+                }
             }
             seg_cp_wait<1>();  // this segment's record has arrived (the next one may be in flight)
             __syncwarp(__activemask());
 
-            // ---- the row: y = H x - beta v_{k-1} at offset t of segment g
             const uint32_t w1 = sw[1];
-            const int zbr = (int)(w1 & 255u), zbl = (int)((w1 >> 8) & 255u);
-            const int zbr4 = (zbr + 3) & ~3, zbl4 = (zbl + 3) & ~3;
-            const uint32_t xm = (lob ^ (w1 >> 16)) & xall;
+            const int zb = (int)(w1 & 255u), zbr = (int)((w1 >> 8) & 255u);
+            const int zb4 = (zb + 3) & ~3;
+            const uint32_t hib = w1 >> 16;
             const T* const xs = xb + base;  // the segment
-            R arr = R(0), ari = R(0), alr = R(0), ali = R(0), hr = R(0), hi = R(0);
-            // exchange bonds below P: partners in the same segment, four loads at a time
-            for (int q0 = 0; q0 < mr4; q0 += 4) {
-                R vr[4], vi[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xs + s_ar[q0 + u][lane], vr[u], vi[u]);
+            for (int h0 = 0; h0 < 2; h0 += NR) {
+                // ---- rows t = window + lane + 32 (h0 + r): y = H x - beta v_{k-1}
+                const T* xt[NR];
+                uint32_t xm[NR];
+                R er[NR], ei[NR], lr[NR], li[NR], hr[NR], hi[NR];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    arr += vr[u];
-                    if constexpr (CPLX) ari += vi[u];
+                for (int r = 0; r < NR; ++r) {
+                    xt[r] = xb + tt[h0 + r];
+                    xm[r] = ((lnw[h0 + r] >> 16) ^ hib) & xall;
+                    er[r] = ei[r] = lr[r] = li[r] = hr[r] = hi[r] = R(0);
                 }
-            }
-            for (int q0 = 0; q0 < ml4; q0 += 4) {
-                R vr[4], vi[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xs + s_al[q0 + u][lane], vr[u], vi[u]);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    alr += vr[u];
-                    if constexpr (CPLX) ali += vi[u];
-                }
-            }
-            // exchange bonds at or above P: the partner segments at the same offset, four at a time
-            for (int q0 = 0; q0 < zbr4; q0 += 4) {
-                R vr[4], vi[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xt + sw[2 + q0 + u], vr[u], vi[u]);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    arr += vr[u];
-                    if constexpr (CPLX) ari += vi[u];
-                }
-            }
-            for (int q0 = 0; q0 < zbl4; q0 += 4) {
-                R vr[4], vi[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) seg_ld<R, CPLX>(xt + sw[2 + RB + q0 + u], vr[u], vi[u]);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    alr += vr[u];
-                    if constexpr (CPLX) ali += vi[u];
-                }
-            }
-            // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
-            for (int c0 = 0; c0 < nX4; c0 += 4) {
-                R vr[4], vi[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int cc = c0 + u;
-                    const uint32_t on = 0u - ((xm >> cc) & 1u);  // all ones when antiparallel (no branch)
-                    const uint32_t o = (on & (sw[xo + cc] + s_xo[cc][lane])) | (~on & (base + (uint32_t)t));
-                    seg_ld<R, CPLX>(xb + o, vr[u], vi[u]);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (c0 + u < nXr) {
-                        arr += vr[u];
-                        if constexpr (CPLX) ari += vi[u];
-                    } else {
-                        alr += vr[u];
-                        if constexpr (CPLX) ali += vi[u];
-                    }
-                }
-            }
-            // the padding read the row itself: take it back out
-            const R off_r = (R)(pad_r + (zbr4 - zbr) + __popc(~xm & xrmask));
-            const R off_l = (R)(pad_l + (zbl4 - zbl) + __popc(~xm & xlmask));
-            arr -= off_r * xr;
-            alr -= off_l * xr;
-            if constexpr (CPLX) {
-                ari -= off_r * xi;
-                ali -= off_l * xi;
-            }
-            // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
-            for (int h0 = 0; h0 < n04 + n124; h0 += 4) {
-                R vr[4], vi[4];
-                if (h0 < n04) {
+                // exchange bonds below P: partners in the same segment, four loads at a time per row
+                for (int q0 = 0; q0 < smax; q0 += 4) {
+                    R vr[NR][4], vi[NR][4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
-                        seg_ld<R, CPLX>(s_stp[h0 + u] + sw[s_soff[h0 + u]] + s_hc[h0 + u][lane], vr[u], vi[u]);
-                } else {
+#pragma unroll
+                        for (int r = 0; r < NR; ++r)
+                            seg_ld<R, CPLX>(xs + (uint32_t)s_al[q0 + u][lane + 32 * (h0 + r)], vr[r][u], vi[r][u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < (int)(cnt[h0 + r] & 255u), vr[r][u], vi[r][u]);
+                }
+                // exchange bonds at or above P: the partner segments at the same offsets, four at a time
+                for (int q0 = 0; q0 < zb4; q0 += 4) {
+                    R vr[NR][4], vi[NR][4];
+                    const uint4 pw = *reinterpret_cast<const uint4*>(sw + 4 + q0);  // 16-byte aligned
+                    const uint32_t pq[4] = {pw.x, pw.y, pw.z, pw.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xt[r] + pq[u], vr[r][u], vi[r][u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr, vr[r][u], vi[r][u]);
+                }
+                // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
+                for (int c0 = 0; c0 < nX4; c0 += 4) {
+                    R vr[NR][4], vi[NR][4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
-                        const uint32_t off = s_soff[h0 + u], hc = s_hc[h0 + u][lane];
-                        const uint32_t r = sw[off + 1 + (hc >> kSegA)] + s_rt[sw[off] | (hc & (kSegLow - 1u))];
-                        seg_ld<R, CPLX>(s_stp[h0 + u] + r, vr[u], vi[u]);
+                        const int cc = c0 + u;
+                        const uint32_t pw = sw[xo + cc];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
+                            const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
+                                               (~on & (base + (uint32_t)tt[h0 + r]));
+                            seg_ld<R, CPLX>(xb + o, vr[r][u], vi[r][u]);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], c0 + u < nXr, vr[r][u], vi[r][u]);
+                }
+                // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
+                for (int h4 = 0; h4 < n04; h4 += 4) {
+                    R vr[NR][4], vi[NR][4];
+                    SegSlot<R, CPLX> S[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        S[u] = s_slot[h4 + u];
+                        const uint32_t sb = sw[S[u].off];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r)
+                            seg_ld<R, CPLX>(S[u].tp + (sb + s_hc[h4 + u][lane + 32 * (h0 + r)]), vr[r][u], vi[r][u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            hr[r] += S[u].cr * vr[r][u];
+                            if constexpr (CPLX) {
+                                hr[r] -= S[u].ci * vi[r][u];
+                                hi[r] += S[u].cr * vi[r][u] + S[u].ci * vr[r][u];
+                            }
+                        }
+                }
+                for (int h4 = n04; h4 < n04 + n124; h4 += 4) {
+                    R vr[NR][4], vi[NR][4];
+                    SegSlot<R, CPLX> S[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        S[u] = s_slot[h4 + u];
+                        const uint32_t ua = sw[S[u].off];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            const uint32_t hc = s_hc[h4 + u][lane + 32 * (h0 + r)];
+                            const uint32_t rr = sw[S[u].off + 1u + (hc >> kSegA)] + s_rt[ua | (hc & (kSegLow - 1u))];
+                            seg_ld<R, CPLX>(S[u].tp + rr, vr[r][u], vi[r][u]);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            hr[r] += S[u].cr * vr[r][u];
+                            if constexpr (CPLX) {
+                                hr[r] -= S[u].ci * vi[r][u];
+                                hi[r] += S[u].cr * vi[r][u] + S[u].ci * vr[r][u];
+                            }
+                        }
+                }
+                if (n0 + n12 < nhop) {
+                    // hops that move more than two low positions above P: the full rank of U | V
+                    const RankTab RT = rank_tab_of(*Sp, Sp->rank_tab);
+#pragma unroll 1
+                    for (int hh = n0 + n12; hh < nhop; ++hh) {
+                        const SegHop<R, CPLX>& F = s_hop[hh];
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) {
+                            const uint32_t V =
+                                seg_perm(lnw[h0 + r] & 0xffffu, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
+                            const uint32_t rr = spin_rank(sw[s_desc.hop_off[hh]] | V, RT, Nd);
+                            R vr, vi;
+                            seg_ld<R, CPLX>(F.tp + rr, vr, vi);
+                            hr[r] += F.cr * vr;
+                            if constexpr (CPLX) {
+                                hr[r] -= F.ci * vi;
+                                hi[r] += F.cr * vi + F.ci * vr;
+                            }
+                        }
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const R cr = s_scr[h0 + u];
-                    hr += cr * vr[u];
-                    if constexpr (CPLX) {
-                        const R ci = s_sci[h0 + u];
-                        hr -= ci * vi[u];
-                        hi += cr * vi[u] + ci * vr[u];
+                for (int r = 0; r < NR; ++r) {
+                    const int hh = h0 + r;
+                    const int nlow = (int)(cnt[hh] >> 8), nr = (int)(cnt[hh] & 255u);
+                    // the padding read the row itself (in split mode into the leg sum; a parallel cross
+                    // bond into its own kind's sum): take it back out; then the diagonal, -J/2 per
+                    // antiparallel bond
+                    const int pads = (smax - nlow) + (zb4 - zb) + __popc(~xm[r] & x4mask & ~(MERGED ? 0u : xrmask));
+                    R h_r, h_i;
+                    if constexpr (MERGED) {
+                        const R e_r = er[r] - (R)pads * xr[hh];
+                        const R e_i = CPLX ? ei[r] - (R)pads * xi[hh] : R(0);
+                        const R diag = -wr * (R)(nlow + zb + __popc(xm[r]));
+                        h_r = wr * e_r + hr[r] + diag * xr[hh];
+                        h_i = CPLX ? wr * e_i + hi[r] + diag * xi[hh] : R(0);
+                    } else {
+                        const R rpad = (R)__popc(~xm[r] & xrmask);
+                        const R a_r = er[r] - rpad * xr[hh], a_i = CPLX ? ei[r] - rpad * xi[hh] : R(0);
+                        const R l_r = lr[r] - (R)pads * xr[hh], l_i = CPLX ? li[r] - (R)pads * xi[hh] : R(0);
+                        const int anr = nr + zbr + __popc(xm[r] & xrmask);
+                        const int anl = (nlow - nr) + (zb - zbr) + __popc(xm[r] & ~xrmask);
+                        const R diag = -(wr * (R)anr + wl * (R)anl);
+                        h_r = wr * a_r + wl * l_r + hr[r] + diag * xr[hh];
+                        h_i = CPLX ? wr * a_i + wl * l_i + hi[r] + diag * xi[hh] : R(0);
+                    }
+                    if (act[hh]) {
+                        const R y_r = h_r - beta * pr[hh];
+                        const R y_i = CPLX ? h_i - beta * pi[hh] : R(0);
+                        st<R, CPLX>(y, (int64_t)base + tt[hh], y_r, y_i);
+                        pend[0] = fma_r(xr[hh], h_r, pend[0]);
+                        pend[1] = fma_r(y_r, y_r, pend[1]);
+                        pend[2] = fma_r(xr[hh], y_r, pend[2]);
+                        pend[3] = fma_r(xr[hh], xr[hh], pend[3]);
+                        if constexpr (CPLX) {
+                            pend[0] = fma_r(xi[hh], h_i, pend[0]);
+                            pend[1] = fma_r(y_i, y_i, pend[1]);
+                            pend[2] = fma_r(xi[hh], y_i, pend[2]);
+                            pend[3] = fma_r(xi[hh], xi[hh], pend[3]);
+                        }
                     }
                 }
             }
-            if (n0 + n12 < nhop) {
-                // hops that move more than two low positions above P: the full rank of U | V
-                const RankTab RT = rank_tab_of(*Sp, Sp->rank_tab);
-#pragma unroll 1
-                for (int h = n0 + n12; h < nhop; ++h) {
-                    const SegHop<R, CPLX>& F = s_hop[h];
-                    const uint32_t V = seg_perm(lo, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                    const uint32_t r = spin_rank(sw[s_desc.hop_off[h]] | V, RT, Nd);
-                    R vr, vi;
-                    seg_ld<R, CPLX>(F.tp + r, vr, vi);
-                    hr += F.cr * vr;
-                    if constexpr (CPLX) {
-                        hr -= F.ci * vi;
-                        hi += F.cr * vi + F.ci * vr;
-                    }
-                }
-            }
-            // diagonal: -J/2 per antiparallel bond
-            const R diag = -(wr * (R)(nr + zbr + __popc(xm & xrmask)) + wl * (R)(nl + zbl + __popc(xm & xlmask)));
-            const R h_r = wr * arr + wl * alr + hr + diag * xr;
-            const R h_i = CPLX ? (wr * ari + wl * ali + hi + diag * xi) : R(0);
-            const R yr = h_r - beta * pr;
-            const R yi = CPLX ? h_i - beta * pi : R(0);
-            st<R, CPLX>(y, (int64_t)base + t, yr, yi);
-            pend[0] = fma_r(xr, h_r, pend[0]);
-            pend[1] = fma_r(yr, yr, pend[1]);
-            pend[2] = fma_r(xr, yr, pend[2]);
-            pend[3] = fma_r(xr, xr, pend[3]);
-            if constexpr (CPLX) {
-                pend[0] = fma_r(xi, h_i, pend[0]);
-                pend[1] = fma_r(yi, yi, pend[1]);
-                pend[2] = fma_r(xi, yi, pend[2]);
-                pend[3] = fma_r(xi, xi, pend[3]);
-            }
-            if (++npend == 4) {
+            npend += 2;
+            if (npend >= 4) {
 #pragma unroll
                 for (int q = 0; q < kReduceSlots; ++q) {
                     fold<R>(acc[q], pend[q]);
@@ -530,10 +614,13 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             }
             __syncwarp(__activemask());  // every lane is done with this buffer before it is refilled
             base = nbase;
-            xr = nxr;
-            xi = nxi;
-            pr = npr;
-            pi = npi;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                xr[h] = nxr[h];
+                xi[h] = nxi[h];
+                pr[h] = npr[h];
+                pi[h] = npi[h];
+            }
         }
         seg_cp_wait<0>();
 #pragma unroll

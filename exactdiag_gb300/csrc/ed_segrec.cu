@@ -31,16 +31,14 @@ __global__ void seg_records_kernel(const SectorView S, const int* __restrict__ f
         const uint32_t zbl = (uint32_t)popc32(d1 & D.ma) + (uint32_t)popc32((Hs ^ (Hs >> 2)) & D.m2);
         uint32_t hib = 0;
         for (int c = 0; c < D.nX; ++c) hib |= ((Hs >> D.cX[c][1]) & 1u) << c;
-        out[1] = zbr | (zbl << 8) | (hib << 16);
-        // padding of the high-bond lists: the segment itself (the kernel takes it back out)
-        for (uint32_t q = zbr; q < ((zbr + 3u) & ~3u); ++q) out[2 + q] = base;
-        for (uint32_t q = zbl; q < ((zbl + 3u) & ~3u); ++q) out[2 + D.RB + q] = base;
+        const uint32_t zb = zbr + zbl;
+        out[1] = zb | (zbr << 8) | (hib << 16);
+        // padding of the high-bond list: the segment itself (the kernel takes it back out)
+        for (uint32_t q = zb; q < ((zb + 3u) & ~3u); ++q) out[4 + q] = base;
         for (int i = 0; i < D.nB; ++i) {
             const uint32_t a = D.bB[i][0], b = D.bB[i][1];
-            if (((Hs >> a) ^ (Hs >> b)) & 1u) {
-                const int pos = seg_high_pos(Hs, i, a, D.nBr, D.nBa, D.mr, D.ma, D.m2);
-                out[i < D.nBr ? 2 + pos : 2 + D.RB + (pos - (int)zbr)] = seg_high_partner(Hs, a, b, kl, R, Nd);
-            }
+            if (((Hs >> a) ^ (Hs >> b)) & 1u)
+                out[4 + seg_high_pos(Hs, i, a, D.nBr, D.nBa, D.mr, D.ma, D.m2)] = seg_high_partner(Hs, a, b, kl, R, Nd);
         }
         for (int c = 0; c < D.nX; ++c) out[D.xo + c] = seg_cross_partner(Hs, D.cX[c][1], kl, P, R, Nd);
         for (int h = 0; h < D.nhop; ++h) {

@@ -1,6 +1,6 @@
 // Host check of the step layout (ed_batch.cu: plan_chunks) on synthetic sectors: row chunks tile
 // every sector's rows, never straddle two blocks and follow the per-kind length rule (pinned on two
-// hand-built sectors as well); segment chunks tile every class and 32-row piece of every free block
+// hand-built sectors as well); segment chunks tile every class and 64-offset window of every free block
 // in whole rounds of the CTA's warps; a sector is cut the same way alone and inside a batch (what keeps batched
 // and sequential recursions bit-identical); every listed block gets one expanded copy, and
 // stabiliser chunks point at their block's copy.  Built with nvcc (the file's kernels are compiled
@@ -164,7 +164,7 @@ int main() {
             // H.v chunks: the same alone and in a batch; segment chunks tile every class of every free block
             expect(alone.hv_count[0] == batch.hv_count[s], "H.v chunk count alone and in a batch", trial, s);
             const int P = secs[s].view.seg_p;
-            // per (block, class, piece): the next segment the chunks must start at
+            // per (block, class, window): the next segment the chunks must start at
             std::vector<std::vector<int64_t>> seg_next(secs[s].spans.size(), std::vector<int64_t>((P + 1) * 8, 0));
             for (int c = 0; c < alone.hv_count[0]; ++c) {
                 const BatchChunk& a = alone.hv[c];
@@ -181,9 +181,9 @@ int main() {
                 expect(a.kl >= 0 && a.kl <= P && a.xoff == 0, "segment chunk class and copies", trial, c);
                 const int64_t nseg = (int64_t)secs[s].host_seg_off[a.kl + 1] - secs[s].host_seg_off[a.kl];
                 const int64_t nA = binom(P, a.kl);
-                const int64_t pieces = (nA + 31) / 32;
+                const int64_t pieces = (nA + kSegWin - 1) / kSegWin;
                 const int64_t round = kSegThreads / 32;
-                expect(a.piece >= 0 && a.piece < pieces, "piece inside the segment", trial, c);
+                expect(a.piece >= 0 && a.piece < pieces, "window inside the segment", trial, c);
                 int64_t& next = seg_next[a.block][a.kl * 8 + a.piece];
                 expect(a.begin == next && a.end > a.begin && a.end <= nseg, "segment chunks tile their class", trial, c);
                 expect(a.end == nseg || (a.end - a.begin) % round == 0, "whole rounds of the CTA's warps", trial, c);
@@ -193,11 +193,11 @@ int main() {
                 if (sp.kind == kRowsFree && sp.count > 0)
                     for (int kl = 0; kl <= P; ++kl) {
                         const int64_t nA = binom(P, kl);
-                        const int64_t pieces = (nA + 31) / 32;
+                        const int64_t pieces = (nA + kSegWin - 1) / kSegWin;
                         for (int64_t pc = 0; pc < pieces; ++pc)
                             expect(seg_next[sp.block][kl * 8 + pc] ==
                                        (int64_t)secs[s].host_seg_off[kl + 1] - secs[s].host_seg_off[kl],
-                                   "every segment piece in a chunk", trial, kl);
+                                   "every segment window in a chunk", trial, kl);
                     }
         }
         // kind lists: every H.v chunk id once, grouped by kind

@@ -48,7 +48,7 @@ UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
 # the kernel generation the committed ncu traffic summary was captured on
-KERNEL_VERSION = "seg_step_kernel v7"
+KERNEL_VERSION = "seg_step_kernel v8"
 TRAFFIC_FILE = ROOT / "profiles" / "seg_step_2x14_traffic.txt"
 
 
@@ -451,7 +451,10 @@ def run_engine(args, rank: int, world: int) -> dict | None:
 
     e2e = None
     if rank == 0:
-        autotune.set_launch(sec, tuned["fp32"]["min_ctas_per_sm"], tuned["fp32"]["ctas_per_sm"])
+        if args.launch:
+            autotune.set_launch(sec, tuned["fp32"]["min_ctas_per_sm"], tuned["fp32"]["ctas_per_sm"])
+        else:
+            autotune.apply(sec, tuned["fp32"])
         e2e = e2e_steps(sec, K, dt32)
 
     extra = {"fp64": {"steps_per_s": world * 1000.0 / ms_fp64, "ms_per_step": ms_fp64, "hv_ms": hv64_ms,
@@ -500,7 +503,7 @@ def run_engine(args, rank: int, world: int) -> dict | None:
         "delta_E_rel": time_to_e0.get("delta_E_rel"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": ncu_traffic(workload_name(SECTOR)),
-                     "kernel": "fused H.v of the step: seg_step_kernel<float,false,MINB> (free blocks) + "
+                     "kernel": "fused H.v of the step: seg_step_kernel<float,false,MINB,true,NR> (free blocks) + "
                                "expand_cand_kernel + lanczos_hv_kernel<float,false,4,1> (stabiliser blocks) + "
                                "lanczos_scalars_kernel (ed_lanczos_hv)",
                      "algorithmic_bytes_per_launch": n * bytes_per_row(s32)},

@@ -1,12 +1,17 @@
-"""Launch-configuration autotuner of the fused Lanczos step.
+"""Autotuner of the fused Lanczos step's launch and work shape.
 
 For a sector shape (L, Nh, Nd, real/complex) and vector dtype it times a few steps for each
-candidate (compiled register variant x persistent grid size, ed_sector_set_launch) and keeps the
-fastest.  Results are cached as JSON keyed by GPU name and shape, so later runs apply the choice
-without timing.  The choice changes only how chunks map onto CTAs: every chunk's partial sums are
-reduced in a fixed order, so results are bitwise identical across candidates.
+candidate and keeps the fastest, in two stages:
 
-Cache file: $EXACTDIAG_GB300_AUTOTUNE, else ~/.cache/exactdiag_gb300/autotune.json.
+1. the free-row kernel's compiled register variant x persistent grid size (ed_sector_set_launch)
+   x rows per lane worked on together (ed_sector_set_step_shape) -- these change only how work maps
+   onto threads and CTAs, never a result bit;
+2. for the winner, the rows of a segment chunk (the unit of work and of the step's partial sums):
+   the sector is re-planned for each candidate, so its recursions' last bits follow the choice (the
+   same for a sector alone and in a batch, which both apply it).
+
+Results are cached as JSON keyed by GPU name and shape, so later runs apply the choice without
+timing.  Cache file: $EXACTDIAG_GB300_AUTOTUNE, else ~/.cache/exactdiag_gb300/autotune.json.
 """
 
 from __future__ import annotations
@@ -22,7 +27,10 @@ import torch
 from exactdiag_gb300 import _native as nat
 from exactdiag_gb300.engine import DeviceSector
 
-CANDIDATES = ((2, 0), (3, 0), (4, 0), (2, 1))
+CANDIDATES = ((2, 0), (3, 0), (4, 0), (2, 1))  # (register variant: min resident CTAs per SM, CTAs per SM)
+ROWS_PER_LANE = (1, 2)
+CHUNK_ROWS = (8192, 16384, 32768)
+DEFAULT_CHUNK_ROWS = 16384
 
 
 def cache_path() -> pathlib.Path:
@@ -60,6 +68,24 @@ def _save(cache: dict) -> None:
 
 def set_launch(sector: DeviceSector, min_ctas: int, ctas: int) -> None:
     nat.check("ed_sector_set_launch", sector._lib.ed_sector_set_launch(sector.handle, int(min_ctas), int(ctas)))
+
+
+def set_step_shape(sector: DeviceSector, rows_per_lane: int, chunk_rows: int) -> None:
+    nat.check("ed_sector_set_step_shape",
+              sector._lib.ed_sector_set_step_shape(sector.handle, int(rows_per_lane), int(chunk_rows)))
+
+
+def get_step_shape(sector: DeviceSector) -> tuple[int, int]:
+    a, c = ctypes.c_int(), ctypes.c_int()
+    nat.check("ed_sector_get_step_shape", sector._lib.ed_sector_get_step_shape(sector.handle, ctypes.byref(a),
+                                                                               ctypes.byref(c)))
+    return a.value, c.value
+
+
+def apply(sector: DeviceSector, rec: dict) -> None:
+    """Set a tuned record's launch and work shape on a sector."""
+    set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+    set_step_shape(sector, rec.get("rows_per_lane", 0), rec.get("chunk_rows", DEFAULT_CHUNK_ROWS))
 
 
 def get_launch(sector: DeviceSector) -> tuple[int, int]:
@@ -107,7 +133,7 @@ def ensure(sector: DeviceSector, weights, dtype: torch.dtype) -> dict | None:
     if rec is None:
         rec = tune(sector, weights, dtype)
     else:
-        set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+        apply(sector, rec)
     return rec
 
 
@@ -122,9 +148,9 @@ def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_
 def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cache: bool) -> dict:
     key = _key(sector, dtype)
     cache = _load() if use_cache else {}
-    if key in cache:
+    if key in cache and "rows_per_lane" in cache[key]:
         rec = cache[key]
-        set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+        apply(sector, rec)
         return dict(rec, cached=True)
     n = sector.n
     v = torch.as_tensor(np.random.default_rng(3).uniform(-1, 1, n), device=sector.device).to(dtype)
@@ -132,12 +158,8 @@ def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cac
     scal = torch.zeros(2 * (steps + 2) + 4, dtype=torch.float64, device=sector.device)
     norm = torch.zeros(1, dtype=torch.float64, device=sector.device)
     sector.normalize(buf[0], norm)
-    timings = {}
-    for minb, ctas in CANDIDATES:
-        try:
-            set_launch(sector, minb, ctas)
-        except nat.EngineError:
-            continue
+
+    def time_steps() -> float:
         for k in range(steps + 1):
             if k == 1:
                 torch.cuda.synchronize()
@@ -147,11 +169,32 @@ def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cac
             sector.lanczos_step(weights, buf[k % 2], other if k else None, other, scal[2 * k: 2 * k + 4])
         stop.record()
         torch.cuda.synchronize()
-        timings[(minb, ctas)] = start.elapsed_time(stop) / steps
+        return start.elapsed_time(stop) / steps
+
+    timings = {}
+    set_step_shape(sector, 0, DEFAULT_CHUNK_ROWS)
+    for minb, ctas in CANDIDATES:
+        for nr in ROWS_PER_LANE:
+            try:
+                set_launch(sector, minb, ctas)
+                set_step_shape(sector, nr, DEFAULT_CHUNK_ROWS)
+            except nat.EngineError:
+                continue
+            timings[(minb, ctas, nr, DEFAULT_CHUNK_ROWS)] = time_steps()
     best = min(timings, key=timings.get)
-    set_launch(sector, *best)
-    rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "ms_per_step": timings[best],
-           "grid": get_launch(sector)[1], "candidates": {f"{a},{b}": t for (a, b), t in timings.items()}}
+    set_launch(sector, best[0], best[1])
+    for rows in CHUNK_ROWS:
+        if rows == DEFAULT_CHUNK_ROWS:
+            continue
+        set_step_shape(sector, best[2], rows)
+        timings[(best[0], best[1], best[2], rows)] = time_steps()
+    best = min(timings, key=timings.get)
+    set_launch(sector, best[0], best[1])
+    set_step_shape(sector, best[2], best[3])
+    rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "rows_per_lane": best[2], "chunk_rows": best[3],
+           "ms_per_step": timings[best], "grid": get_launch(sector)[1],
+           "candidates": {f"{a},{b},{c},{d}": t for (a, b, c, d), t in timings.items()},
+           "candidate_key": "min_ctas_per_sm,ctas_per_sm,rows_per_lane,chunk_rows"}
     cache[key] = rec
     if use_cache:
         _save(cache)

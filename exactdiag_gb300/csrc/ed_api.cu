@@ -148,6 +148,18 @@ int ed_sector_get_launch(const ed_sector* h, int* min_ctas_per_sm, int* grid) {
     return ED_OK;
 }
 
+int ed_sector_set_step_shape(ed_sector* h, int rows_per_lane, int chunk_rows) {
+    if (!h) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: NULL sector");
+    return set_step_shape(h->s, rows_per_lane, chunk_rows);
+}
+
+int ed_sector_get_step_shape(const ed_sector* h, int* rows_per_lane, int* chunk_rows) {
+    if (!h || !rows_per_lane || !chunk_rows) return set_error(ED_ERR_INVALID, "ed_sector_get_step_shape: NULL argument");
+    *rows_per_lane = h->s.seg_nr;
+    *chunk_rows = h->s.seg_chunk_rows;
+    return ED_OK;
+}
+
 int ed_position_correlations(const ed_sector* h, int dtype, const void* psi_dev, int kind, int nfixed,
                              const int* fixed_shifts, double* out_host, void* stream) {
     if (!h || !psi_dev || !out_host) return set_error(ED_ERR_INVALID, "ed_position_correlations: NULL argument");

@@ -1,22 +1,17 @@
 // ed_step_free.cu -- fused step kernel for rows of blocks with a trivial stabiliser (the bulk of
-// every doped sector): the segment kernel of ed_seg.cuh when rung and leg J agree, in three register
-// budgets (2, 3 or 4 resident CTAs per SM).  Real and complex FP32 vectors take two rows per lane
-// together, FP64 ones one at a time.  Unequal rung and leg J take ed_step_free_split.cu.
+// every doped sector): the segment kernel of ed_seg.cuh when rung and leg J agree, a lane's two rows
+// worked on together, in three register budgets (2, 3 or 4 resident CTAs per SM).  One row at a
+// time: ed_step_free_nr1.cu; unequal rung and leg J: ed_step_free_split.cu.
 #include "ed_seg.cuh"
 
 namespace ed {
-
-template <typename R, bool CPLX>
-constexpr int seg_rows() {
-    return sizeof(R) == 4 ? 2 : 1;
-}
 
 namespace {
 
 template <typename R, bool CPLX, int MINB>
 int launch_seg(const StepArgs& a, cudaStream_t st) {
     if (a.count <= 0) return ED_OK;
-    auto* kern = seg_step_kernel<R, CPLX, MINB, true, seg_rows<R, CPLX>()>;
+    auto* kern = seg_step_kernel<R, CPLX, MINB, true, 2>;
     const int grid = a.grid < a.count ? a.grid : a.count;
     kern<<<grid, kSegThreads, 0, st>>>(a.views, a.offs, a.chunks, a.idx, a.count, a.w, a.v, a.vprev, a.other, a.first,
                                        a.scal, a.stride, a.k, a.partials, a.xfull);
@@ -47,11 +42,11 @@ int seg_occupancy() {
 
 }  // namespace
 
-int step_hv_free_split(int dtype, const StepArgs& a, cudaStream_t st);
-
-int step_hv_free(int dtype, int minb, const StepArgs& a, cudaStream_t st) {
+int step_hv_free(int dtype, int minb, int nr, const StepArgs& a, cudaStream_t st) {
+    nr = seg_rows_for(dtype, nr);
     // one exchange coefficient when J_rung = J_leg (the sums need no per-element choice)
-    if (a.w.w[2] != a.w.w[3]) return step_hv_free_split(dtype, a, st);
+    if (a.w.w[2] != a.w.w[3]) return step_hv_free_split(dtype, nr, a, st);
+    if (nr == 1) return step_hv_free_nr1(dtype, minb, a, st);
     if (minb == 2) return seg_dtype<2>(dtype, a, st);
     if (minb == 4) return seg_dtype<4>(dtype, a, st);
     return seg_dtype<3>(dtype, a, st);

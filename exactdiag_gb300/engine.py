@@ -240,7 +240,10 @@ def batch_lanczos(sectors: list, weights, v0s: list, num_lanczos_vecs: int, use_
     m = int(num_lanczos_vecs)
     nsec = len(sectors)
     stride = 2 * m + 4
-    autotune.ensure(sectors[0], weights, v0s[0].dtype)  # the batch runs with the first sector's launch
+    # every sector gets its tuned work shape (its plan, as when it runs alone); the batch launches with
+    # the first sector's launch
+    for s in sectors[::-1]:
+        autotune.ensure(s, weights, v0s[0].dtype)
     dev = sectors[0].device
     coef = torch.zeros(nsec * stride, dtype=torch.float64, device=dev)
     code = _CODE_OF_TORCH[v0s[0].dtype]

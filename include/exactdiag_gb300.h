@@ -55,11 +55,21 @@ int ed_sector_destroy(ed_sector* s);
 int ed_basis_build(ed_sector* s, void* stream);
 
 /* Launch configuration of the fused Lanczos step (tuning; no reference counterpart):
- * min_ctas_per_sm selects the compiled variant (3 or 4 resident CTAs per SM, i.e. a register
- * budget of 85 or 64 per thread) and ctas_per_sm the persistent grid (0 = as many as fit).
- * exactdiag_gb300.autotune times the candidates and caches the fastest per sector shape. */
+ * min_ctas_per_sm selects the compiled variant of the free-row kernel (2, 3 or 4 resident CTAs per
+ * SM, i.e. a register budget of 128, 80 or 64 per thread) and ctas_per_sm the persistent grid (0 =
+ * as many as fit).  exactdiag_gb300.autotune times the candidates and caches the fastest per sector
+ * shape.  Results do not depend on these two. */
 int ed_sector_set_launch(ed_sector* s, int min_ctas_per_sm, int ctas_per_sm);
 int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
+
+/* Work shape of the free-row kernel (tuning; no reference counterpart): rows_per_lane, the rows of
+ * a segment each lane works on together (1 or 2; 0 = two for FP32 vectors, one for FP64), and
+ * chunk_rows, the rows of one chunk of work (a power of two in [4096, 65536]; default 16384).  The
+ * rows per lane do not change results; a new chunk length re-plans the sector, and since the step's
+ * partial sums are kept per chunk, its recursions then differ in the last bits (a sector still gives
+ * the same bits alone and in a batch).  ED_ERR_INVALID for values out of range. */
+int ed_sector_set_step_shape(ed_sector* s, int rows_per_lane, int chunk_rows);
+int ed_sector_get_step_shape(const ed_sector* s, int* rows_per_lane, int* chunk_rows);
 
 /* Chunks of the sector's fused step per row kind: counts[0] chunks of rows of blocks with a
  * trivial stabiliser (colex-delta rows), counts[1] chunks of rows of blocks with a small

@@ -77,3 +77,50 @@ def test_step_kernel_vs_oracle_weights(cuda, oracle, key, w):
 def test_step_kernel_equals_hv_2x12_all_sectors(cuda, precision):
     for key in FULL:
         _check(cuda, key, precision, 1e-12 if precision == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("key", [(12, 2, 11, 0, 0), (12, 2, 11, 5, 1)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_step_shapes(cuda, key, precision):
+    """Every launch variant and rows-per-lane choice gives the same bits; every chunk length gives
+    the step kernel's y = H v (the one-thread-per-row H v, to the form's tolerance), and a sector
+    re-planned back to its first chunk length gives its first bits again."""
+    torch = cuda
+    from exactdiag_gb300 import _native as nat
+    from exactdiag_gb300 import autotune
+    from exactdiag_gb300.engine import DeviceSector
+
+    sec = DeviceSector(*key)
+    dt = sec.dtype(precision)
+    x = seeded_vector(sec.n, 23, not sec.is_real)
+    v = torch.as_tensor(x if not sec.is_real else x.real, device=sec.device).to(dt)
+    ref = sec.hv_mode(v, W, 0)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    scale = max(1.0, float(torch.max(torch.abs(ref)).item()))
+
+    def step():
+        y = torch.zeros_like(v)
+        scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
+        sec.lanczos_hv(W, v, None, y, scal[0:4])
+        torch.cuda.synchronize()
+        return y, scal[:4].cpu().numpy()
+
+    first_y, first_s = step()
+    for minb, ctas in autotune.CANDIDATES:
+        for nr in (1, 2):
+            autotune.set_launch(sec, minb, ctas)
+            autotune.set_step_shape(sec, nr, autotune.DEFAULT_CHUNK_ROWS)
+            y, s = step()
+            assert torch.equal(y, first_y) and np.array_equal(s, first_s), (minb, ctas, nr)
+    for rows in (4096, 8192, 32768, 65536):
+        autotune.set_step_shape(sec, 0, rows)
+        assert autotune.get_step_shape(sec) == (0, rows)
+        y, s = step()
+        assert float(torch.max(torch.abs(y - ref)).item()) <= tol * scale, rows
+        assert abs(s[1] - first_s[1]) <= 1e-9 * max(1.0, abs(first_s[1])) * (1 if precision == "fp64" else 1e3)
+    autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS)
+    y, s = step()
+    assert torch.equal(y, first_y) and np.array_equal(s, first_s)
+    for bad in ((3, 16384), (-1, 16384), (1, 12288), (1, 2048), (2, 131072)):
+        with pytest.raises(nat.EngineError):
+            autotune.set_step_shape(sec, *bad)

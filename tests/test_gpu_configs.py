@@ -67,6 +67,48 @@ def test_2x12_szq_spectra_batched_equals_sequential(cuda, in_tmp):
     assert diff <= 1e-6
 
 
+def _fp32_error_and_truncation(torch, src_key, dst_key, op, ws, eta, ms, m_ref):
+    """For each m: (complex64 vs complex128 L1 spectrum difference at equal m, the complex128
+    recursion's own truncation error against m_ref steps), both relative to the complex128 L1 norm."""
+    from exactdiag_gb300.eigensolver import lowest_eigenpairs
+    from exactdiag_gb300.engine import DeviceSector, continued_fraction
+    from exactdiag_gb300.lanczos import lanczos_coefficients
+
+    src = DeviceSector(*src_key)
+    vals, vecs = lowest_eigenpairs(src, W, 1)
+    e0 = float(vals[0])
+    gs = torch.as_tensor(vecs[:, 0], device="cuda")
+    dst = DeviceSector(*dst_key)
+    phi = src.excite_into(dst, op, dst_key[3], dst_key[4], 0, gs)
+    dev = lambda v: torch.as_tensor(np.asarray(v, np.float64), device="cuda")  # noqa: E731
+
+    def spectrum(x, m):
+        a, b, nrm = lanczos_coefficients(dst, W, x, m)
+        return continued_fraction(dev(a), dev(b), dev(ws + e0), 0.0, eta, nrm ** 2).cpu().numpy()
+
+    ref = spectrum(phi, m_ref)
+    out = []
+    for m in ms:
+        s64, s32 = spectrum(phi, m), spectrum(phi.to(torch.complex64), m)
+        out.append((m, float(np.sum(np.abs(s32 - s64)) / np.sum(np.abs(s64))),
+                    float(np.sum(np.abs(s64 - ref)) / np.sum(np.abs(ref)))))
+    return out
+
+
+@pytest.mark.parametrize("dst", [(12, 2, 11, 3, 0), (12, 2, 11, 6, 1)])
+def test_2x12_szq_complex64_error_within_truncation(cuda, dst):
+    """The complex64 recursion (FP64 reductions) adds an error of the order of the continued
+    fraction's own truncation error at the same length, and both fall together with m: the FP32
+    form is as good as the method at that m.  Measured ratios 0.3-2.0 over 5 targets and m = 25-200
+    (2x12 S^z_q and undoped 2x14 c_minus); the bound allows 3."""
+    rows = _fp32_error_and_truncation(cuda, (12, 2, 11, 0, 0), dst, "Szq", np.linspace(0, 6, 2000), 0.05,
+                                      (100, 150, 200), 300)
+    for m, d32, t64 in rows:
+        print(f"2x12 Szq {dst}: m={m} complex64 vs complex128 L1 {d32:.2e}, truncation vs m=300 {t64:.2e}")
+        assert d32 <= 3.0 * t64, (m, d32, t64)
+    assert rows[-1][1] < rows[0][1]  # the FP32 error falls with m
+
+
 def test_undoped_2x14_spectral_function_minus_mixed_vs_fp64(cuda, in_tmp):
     from exactdiag_gb300.tJ_spin_half_ladder import api
 
@@ -86,8 +128,18 @@ def test_undoped_2x14_spectral_function_minus_mixed_vs_fp64(cuda, in_tmp):
         print(f"  q {q}: max {np.max(d[q]) / max(np.max(f), 1e-300):.2e}  L1 {np.sum(d[q]) / max(np.sum(f[q]), 1e-300):.2e}"
               f"  weight {np.sum(f[q]):.3e}")
     # complex64 vectors through 200 unreorthogonalised recursion steps: a few percent of the peak,
-    # the size of the FP64 recursion's own truncation error at this length (m=150 against m=200)
+    # the size of the FP64 recursion's own truncation error at this length (the next test pins that)
     assert rel <= 5e-2 and l1 <= 5e-2
+
+
+def test_undoped_2x14_c_minus_complex64_error_within_truncation(cuda):
+    """The same bound as for the 2x12 S^z_q spectra on config 4's c_minus: the complex64 error at
+    m = 200 is of the order of the complex128 recursion's truncation error against m = 300."""
+    rows = _fp32_error_and_truncation(cuda, (14, 0, 14, 0, 0), (14, 1, 13, 3, 0), "spectral_function_minus",
+                                      np.linspace(-4, 8, 4000), 0.05, (100, 200), 300)
+    for m, d32, t64 in rows:
+        print(f"undoped 2x14 c_minus q=(3,0): m={m} complex64 vs complex128 L1 {d32:.2e}, truncation {t64:.2e}")
+        assert d32 <= 3.0 * t64, (m, d32, t64)
 
 
 def test_undoped_2x14_spectral_function_minus_batched_equals_sequential(cuda, in_tmp):

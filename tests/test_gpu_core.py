@@ -123,7 +123,7 @@ def test_hv_deterministic(torch):
 
 
 def test_lanczos_coefficients_vs_golden(torch, golden_sectors):
-    from exactdiag_gb300.lanczos import lanczos_coefficients
+    from exactdiag_gb300.lanczos import lanczos_coefficients, tridiagonal_eigvals
 
     w = dict(zip(("tl", "tr", "jl", "jr"), golden_sectors["weights"]))
     for key in golden_sectors["sectors"]:
@@ -140,6 +140,14 @@ def test_lanczos_coefficients_vs_golden(torch, golden_sectors):
             assert np.max(np.abs(a[:k] - ga[:k])) < 1e-9
             assert np.max(np.abs(b[:k] - gb[:k])) < 1e-9
             assert abs(nrm - np.linalg.norm(v0)) < 1e-10
+            # past step 12 the coefficients themselves drift apart (two FP64 runs that differ in the last
+            # bit of a dot product diverge roughly threefold per step once Ritz values converge), but what
+            # the whole recursion computes is pinned: the extremal eigenvalues of the 30-step tridiagonal
+            # matrix, which converge to eigenvalues of H in both runs
+            ritz, gritz = tridiagonal_eigvals(a, b), tridiagonal_eigvals(ga, gb)
+            scale = max(1.0, float(np.max(np.abs(gritz))))
+            assert abs(ritz[0] - gritz[0]) <= 1e-10 * scale, (tag, ritz[0], gritz[0])
+            assert abs(ritz[-1] - gritz[-1]) <= 1e-10 * scale, (tag, ritz[-1], gritz[-1])
 
 
 def test_continued_fraction_vs_oracle(torch, oracle):

@@ -29,7 +29,7 @@ from exactdiag_gb300.engine import DeviceSector
 
 CANDIDATES = ((2, 0), (3, 0), (4, 0), (2, 1))  # (register variant: min resident CTAs per SM, CTAs per SM)
 ROWS_PER_LANE = (1, 2)
-CHUNK_ROWS = (8192, 16384, 32768)
+CHUNK_ROWS = (2048, 4096, 8192, 16384, 32768)
 DEFAULT_CHUNK_ROWS = 16384
 
 

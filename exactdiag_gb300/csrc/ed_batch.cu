@@ -794,12 +794,12 @@ int set_launch(Sector& s, int minb, int ctas_per_sm) {
 }
 
 // Rows per lane of the free-row kernel (1, 2, or 0 = by dtype) and the rows of a segment chunk (a power
-// of two from 4096 to 65536).  A new chunk length re-plans the sector's steps: its per-chunk sums,
+// of two from 1024 to 65536).  A new chunk length re-plans the sector's steps: its per-chunk sums,
 // and with them the last bits of its recursions, follow the plan (the same alone and in a batch).
 int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows) {
     if (rows_per_lane < 0 || rows_per_lane > 2) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: rows per lane");
-    if (chunk_rows < 4096 || chunk_rows > 65536 || (chunk_rows & (chunk_rows - 1)))
-        return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: chunk rows must be a power of two in [4096, 65536]");
+    if (chunk_rows < 1024 || chunk_rows > 65536 || (chunk_rows & (chunk_rows - 1)))
+        return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: chunk rows must be a power of two in [1024, 65536]");
     s.seg_nr = rows_per_lane;
     if (chunk_rows == s.seg_chunk_rows) return ED_OK;
     s.seg_chunk_rows = chunk_rows;

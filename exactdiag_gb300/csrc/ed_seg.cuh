@@ -243,6 +243,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     const R wr = R(0.5) * (R)W.w[3], wl = R(0.5) * (R)W.w[2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
+    // the chunk whose tables the shared memory holds: a CTA's next chunk of the same (sector, block,
+    // class, window) keeps them (with the grid a multiple of the windows of a range, a CTA's chunks
+    // share their window and mostly their block and class)
+    int held_sec = -1, held_block = -1, held_kl = -1, held_piece = -1;
     for (int c = blockIdx.x; c < count; c += gridDim.x) {
         const int cid = idx[c];
         const BatchChunk ch = chunks[cid];
@@ -252,112 +256,120 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int nA = (int)comb[kl * kCombStride + P];
         const int win = kSegWin * ch.piece;
         const int nact = min(32, nA - win);  // lanes with a first row
+        const bool held = ch.sec == held_sec && ch.block == held_block && kl == held_kl && ch.piece == held_piece;
+        held_sec = ch.sec;
+        held_block = ch.block;
+        held_kl = kl;
+        held_piece = ch.piece;
         __syncthreads();  // the previous chunk's rows are done with the shared tables
-        {
+        if (!held) {
             const uint4* src = reinterpret_cast<const uint4*>(Sp->seg + ch.block);
             uint4* dst = reinterpret_cast<uint4*>(&s_desc);
             for (int i = threadIdx.x; i < (int)(sizeof(SegDesc) / 16); i += blockDim.x) dst[i] = src[i];
+            __syncthreads();
         }
-        __syncthreads();
         const int nhop = s_desc.nhop, n0 = s_desc.n0, n12 = s_desc.n12, nX = s_desc.nX, nXr = s_desc.nXr;
         const int64_t bstart = s_desc.start;
         T* const x = reinterpret_cast<T*>(v) + offs[ch.sec];
         const T* const xb = x + bstart;
-        if (warp == 2 && lane < kMaxHops) {
-            // every hop gets a record: absent hops (and those past nhop) read a valid element with
-            // coefficient 0
-            const int h = lane;
-            SegHop<R, CPLX>& F = s_hop[h];
-            const SegHopDesc& G = s_desc.hop[h];
-            const bool live = h < nhop && G.kind != 3 && W.w[G.term] != 0.0;
-            F.keep = G.keep;
-            F.band = G.band;
-            F.sl = G.sl;
-            F.sr = G.sr;
-            F.p = G.p;
-            F.q = G.q;
-            F.swap = G.swap;
-            F.rot = G.rot;
-            F.nsr = G.nsr;
-            F.nb = h < nhop ? G.nb : 0u;
-            F.bp0 = G.bpos[0];
-            F.bp1 = G.bpos[1];
-            F.kind = live ? (uint32_t)G.kind : 3u;
-            F.tp = xb;
-            F.cr = F.ci = R(0);
-            if (live) {
-                const R w = (R)W.w[G.term];
-                const R sw = G.sign ? -w : w;
-                R cf = sw;
-                if (G.kind == 1) {
-                    cf = sw * (R)sqrt((double)N);
-                    F.tp = reinterpret_cast<const T*>(xfull) + ch.xoff +
-                           G.tstart * (int64_t)comb[Nd * kCombStride + Ns];
-                } else {
-                    F.tp = x + G.tstart;
-                }
-                double sn, cs;
-                sincospi((double)G.e / (double)L, &sn, &cs);
-                if constexpr (CPLX) {
-                    F.cr = cf * (R)cs;
-                    F.ci = cf * (R)sn;
-                } else {
-                    F.cr = G.e == 0 ? cf : -cf;
-                }
-            }
-        }
-        // the offset whose terms column j holds: its own, or (past the class's rows) column j - 32's
-        const int jcol = 32 * warp + lane;  // warps 0 and 1
-        int tsrc = win + jcol;
-        if (warp < 2 && tsrc >= nA) tsrc = (win + lane < nA) ? win + lane : win;
-        const uint32_t lo_c = (warp < 2 && tsrc < nA) ? s_ut[s_utoff[kl] + tsrc] : 0u;
-        if (warp < 2) {
-            // bonds below P: the antiparallel ones' partners, rung bonds first, padded with the offset
-            // itself up to the table's length (read in fours, the padding taken back out after the sums)
-            int nr = 0, nlow = 0;
-            const int nAb = s_desc.nA, nAr = s_desc.nAr;
-            for (int i = 0; i < nAb; ++i) {
-                const uint32_t f = s_desc.fA[i], sb = lo_c & f;
-                if (sb != 0u && sb != f) {
-                    s_al[nlow++][jcol] = s_rt[lo_c ^ f];
-                    if (i < nAr) ++nr;
+        if (!held) {  // the chunk's tables: hop records, per-offset terms, hop slots
+            if (warp == 2 && lane < kMaxHops) {
+                // every hop gets a record: absent hops (and those past nhop) read a valid element with
+                // coefficient 0
+                const int h = lane;
+                SegHop<R, CPLX>& F = s_hop[h];
+                const SegHopDesc& G = s_desc.hop[h];
+                const bool live = h < nhop && G.kind != 3 && W.w[G.term] != 0.0;
+                F.keep = G.keep;
+                F.band = G.band;
+                F.sl = G.sl;
+                F.sr = G.sr;
+                F.p = G.p;
+                F.q = G.q;
+                F.swap = G.swap;
+                F.rot = G.rot;
+                F.nsr = G.nsr;
+                F.nb = h < nhop ? G.nb : 0u;
+                F.bp0 = G.bpos[0];
+                F.bp1 = G.bpos[1];
+                F.kind = live ? (uint32_t)G.kind : 3u;
+                F.tp = xb;
+                F.cr = F.ci = R(0);
+                if (live) {
+                    const R w = (R)W.w[G.term];
+                    const R sw = G.sign ? -w : w;
+                    R cf = sw;
+                    if (G.kind == 1) {
+                        cf = sw * (R)sqrt((double)N);
+                        F.tp = reinterpret_cast<const T*>(xfull) + ch.xoff +
+                               G.tstart * (int64_t)comb[Nd * kCombStride + Ns];
+                    } else {
+                        F.tp = x + G.tstart;
+                    }
+                    double sn, cs;
+                    sincospi((double)G.e / (double)L, &sn, &cs);
+                    if constexpr (CPLX) {
+                        F.cr = cf * (R)cs;
+                        F.ci = cf * (R)sn;
+                    } else {
+                        F.cr = G.e == 0 ? cf : -cf;
+                    }
                 }
             }
-            for (int q = nlow; q < kSegLowMax; ++q) s_al[q][jcol] = (uint8_t)tsrc;
-            const int mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow);
-            uint32_t lob = 0;
-            for (int cc = 0; cc < kSegMaxX; ++cc) {
-                const uint32_t a = s_desc.cX[cc][0];
-                if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
-                s_xo[cc][jcol] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
+            // the offset whose terms column j holds: its own, or (past the class's rows) column j - 32's
+            const int jcol = 32 * warp + lane;  // warps 0 and 1
+            int tsrc = win + jcol;
+            if (warp < 2 && tsrc >= nA) tsrc = (win + lane < nA) ? win + lane : win;
+            const uint32_t lo_c = (warp < 2 && tsrc < nA) ? s_ut[s_utoff[kl] + tsrc] : 0u;
+            if (warp < 2) {
+                // bonds below P: the antiparallel ones' partners, rung bonds first, padded with the offset
+                // itself up to the table's length (read in fours, the padding taken back out after the sums)
+                int nr = 0, nlow = 0;
+                const int nAb = s_desc.nA, nAr = s_desc.nAr;
+                for (int i = 0; i < nAb; ++i) {
+                    const uint32_t f = s_desc.fA[i], sb = lo_c & f;
+                    if (sb != 0u && sb != f) {
+                        s_al[nlow++][jcol] = s_rt[lo_c ^ f];
+                        if (i < nAr) ++nr;
+                    }
+                }
+                for (int q = nlow; q < kSegLowMax; ++q) s_al[q][jcol] = (uint8_t)tsrc;
+                const int mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow);
+                uint32_t lob = 0;
+                for (int cc = 0; cc < kSegMaxX; ++cc) {
+                    const uint32_t a = s_desc.cX[cc][0];
+                    if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
+                    s_xo[cc][jcol] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
+                }
+                s_lane[jcol] = lo_c | (lob << 16);
+                s_cnt[jcol] = (uint32_t)nr | ((uint32_t)nlow << 8);
+                if (lane == 0) s_maxw[warp] = (mx + 3) & ~3;
             }
-            s_lane[jcol] = lo_c | (lob << 16);
-            s_cnt[jcol] = (uint32_t)nr | ((uint32_t)nlow << 8);
-            if (lane == 0) s_maxw[warp] = (mx + 3) & ~3;
-        }
-        __syncthreads();
-        const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
-        if (warp < 2) {
-            for (int sl = 0; sl < n04 + n124; ++sl) {
+            __syncthreads();
+            const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
+            if (warp < 2) {
+                for (int sl = 0; sl < n04 + n124; ++sl) {
+                    const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
+                    uint32_t hc = 0;
+                    if (h >= 0 && s_hop[h].kind != 3) {
+                        const SegHop<R, CPLX>& F = s_hop[h];
+                        const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
+                        hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
+                    }
+                    s_hc[sl][jcol] = (uint16_t)hc;
+                }
+            } else if (warp == 2 && lane < n04 + n124) {
+                const int sl = lane;
                 const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
-                uint32_t hc = 0;
-                if (h >= 0 && s_hop[h].kind != 3) {
-                    const SegHop<R, CPLX>& F = s_hop[h];
-                    const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                    hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
-                }
-                s_hc[sl][jcol] = (uint16_t)hc;
+                SegSlot<R, CPLX>& S = s_slot[sl];
+                S.tp = h >= 0 ? s_hop[h].tp : xb;
+                S.cr = h >= 0 ? s_hop[h].cr : R(0);
+                if constexpr (CPLX) S.ci = h >= 0 ? s_hop[h].ci : R(0);
+                S.off = h >= 0 ? s_desc.hop_off[h] : s_desc.zero_w;
             }
-        } else if (warp == 2 && lane < n04 + n124) {
-            const int sl = lane;
-            const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
-            SegSlot<R, CPLX>& S = s_slot[sl];
-            S.tp = h >= 0 ? s_hop[h].tp : xb;
-            S.cr = h >= 0 ? s_hop[h].cr : R(0);
-            if constexpr (CPLX) S.ci = h >= 0 ? s_hop[h].ci : R(0);
-            S.off = h >= 0 ? s_desc.hop_off[h] : s_desc.zero_w;
+            __syncthreads();
         }
-        __syncthreads();
+        const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
 
         const int smax = max(s_maxw[0], s_maxw[1]);  // low lists read, in fours
         const uint32_t rec_len = s_desc.rec_len, xo = s_desc.xo;

@@ -64,7 +64,7 @@ int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
 
 /* Work shape of the free-row kernel (tuning; no reference counterpart): rows_per_lane, the rows of
  * a segment each lane works on together (1 or 2; 0 = two for FP32 vectors, one for FP64), and
- * chunk_rows, the rows of one chunk of work (a power of two in [4096, 65536]; default 16384).  The
+ * chunk_rows, the rows of one chunk of work (a power of two in [1024, 65536]; default 16384).  The
  * rows per lane do not change results; a new chunk length re-plans the sector, and since the step's
  * partial sums are kept per chunk, its recursions then differ in the last bits (a sector still gives
  * the same bits alone and in a batch).  ED_ERR_INVALID for values out of range. */

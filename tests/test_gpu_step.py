@@ -112,7 +112,7 @@ def test_step_shapes(cuda, key, precision):
             autotune.set_step_shape(sec, nr, autotune.DEFAULT_CHUNK_ROWS)
             y, s = step()
             assert torch.equal(y, first_y) and np.array_equal(s, first_s), (minb, ctas, nr)
-    for rows in (4096, 8192, 32768, 65536):
+    for rows in (1024, 4096, 8192, 32768, 65536):
         autotune.set_step_shape(sec, 0, rows)
         assert autotune.get_step_shape(sec) == (0, rows)
         y, s = step()
@@ -121,6 +121,6 @@ def test_step_shapes(cuda, key, precision):
     autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS)
     y, s = step()
     assert torch.equal(y, first_y) and np.array_equal(s, first_s)
-    for bad in ((3, 16384), (-1, 16384), (1, 12288), (1, 2048), (2, 131072)):
+    for bad in ((3, 16384), (-1, 16384), (1, 12288), (1, 512), (2, 131072)):
         with pytest.raises(nat.EngineError):
             autotune.set_step_shape(sec, *bad)

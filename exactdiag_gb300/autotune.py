@@ -4,8 +4,9 @@ For a sector shape (L, Nh, Nd, real/complex) and vector dtype it times a few ste
 candidate and keeps the fastest, in two stages:
 
 1. the free-row kernel's compiled register variant x persistent grid size (ed_sector_set_launch)
-   x rows per lane worked on together (ed_sector_set_step_shape) -- these change only how work maps
-   onto threads and CTAs, never a result bit;
+   x rows per lane worked on together, and the variant whose gathers go through shared memory
+   (ed_sector_set_step_shape) -- these change only how work maps onto threads and CTAs, never a
+   result bit;
 2. for the winner, the rows of a segment chunk (the unit of work and of the step's partial sums):
    the sector is re-planned for each candidate, so its recursions' last bits follow the choice (the
    same for a sector alone and in a batch, which both apply it).
@@ -29,6 +30,8 @@ from exactdiag_gb300.engine import DeviceSector
 
 CANDIDATES = ((2, 0), (3, 0), (4, 0), (2, 1))  # (register variant: min resident CTAs per SM, CTAs per SM)
 ROWS_PER_LANE = (1, 2)
+# gathers through shared memory (cp.async): one compiled variant of 2 CTAs per SM, all that fit
+STAGED_CANDIDATES = ((2, 0, 1), (2, 0, 2))  # (register variant, CTAs per SM, rows per lane)
 CHUNK_ROWS = (2048, 4096, 8192, 16384, 32768)
 DEFAULT_CHUNK_ROWS = 16384
 
@@ -70,22 +73,23 @@ def set_launch(sector: DeviceSector, min_ctas: int, ctas: int) -> None:
     nat.check("ed_sector_set_launch", sector._lib.ed_sector_set_launch(sector.handle, int(min_ctas), int(ctas)))
 
 
-def set_step_shape(sector: DeviceSector, rows_per_lane: int, chunk_rows: int) -> None:
+def set_step_shape(sector: DeviceSector, rows_per_lane: int, chunk_rows: int, staged: int = 0) -> None:
     nat.check("ed_sector_set_step_shape",
-              sector._lib.ed_sector_set_step_shape(sector.handle, int(rows_per_lane), int(chunk_rows)))
+              sector._lib.ed_sector_set_step_shape(sector.handle, int(rows_per_lane), int(chunk_rows), int(staged)))
 
 
-def get_step_shape(sector: DeviceSector) -> tuple[int, int]:
-    a, c = ctypes.c_int(), ctypes.c_int()
+def get_step_shape(sector: DeviceSector) -> tuple[int, int, int]:
+    a, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     nat.check("ed_sector_get_step_shape", sector._lib.ed_sector_get_step_shape(sector.handle, ctypes.byref(a),
-                                                                               ctypes.byref(c)))
-    return a.value, c.value
+                                                                               ctypes.byref(c), ctypes.byref(g)))
+    return a.value, c.value, g.value
 
 
 def apply(sector: DeviceSector, rec: dict) -> None:
     """Set a tuned record's launch and work shape on a sector."""
     set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
-    set_step_shape(sector, rec.get("rows_per_lane", 0), rec.get("chunk_rows", DEFAULT_CHUNK_ROWS))
+    set_step_shape(sector, rec.get("rows_per_lane", 0), rec.get("chunk_rows", DEFAULT_CHUNK_ROWS),
+                   rec.get("staged", 0))
 
 
 def get_launch(sector: DeviceSector) -> tuple[int, int]:
@@ -148,7 +152,7 @@ def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_
 def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cache: bool) -> dict:
     key = _key(sector, dtype)
     cache = _load() if use_cache else {}
-    if key in cache and "rows_per_lane" in cache[key]:
+    if key in cache and "staged" in cache[key]:
         rec = cache[key]
         apply(sector, rec)
         return dict(rec, cached=True)
@@ -173,28 +177,29 @@ def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cac
 
     timings = {}
     set_step_shape(sector, 0, DEFAULT_CHUNK_ROWS)
-    for minb, ctas in CANDIDATES:
-        for nr in ROWS_PER_LANE:
-            try:
-                set_launch(sector, minb, ctas)
-                set_step_shape(sector, nr, DEFAULT_CHUNK_ROWS)
-            except nat.EngineError:
-                continue
-            timings[(minb, ctas, nr, DEFAULT_CHUNK_ROWS)] = time_steps()
+    shapes = [(minb, ctas, nr, 0) for minb, ctas in CANDIDATES for nr in ROWS_PER_LANE]
+    shapes += [(minb, ctas, nr, 1) for minb, ctas, nr in STAGED_CANDIDATES]
+    for minb, ctas, nr, staged in shapes:
+        try:
+            set_launch(sector, minb, ctas)
+            set_step_shape(sector, nr, DEFAULT_CHUNK_ROWS, staged)
+        except nat.EngineError:
+            continue
+        timings[(minb, ctas, nr, staged, DEFAULT_CHUNK_ROWS)] = time_steps()
     best = min(timings, key=timings.get)
     set_launch(sector, best[0], best[1])
     for rows in CHUNK_ROWS:
         if rows == DEFAULT_CHUNK_ROWS:
             continue
-        set_step_shape(sector, best[2], rows)
-        timings[(best[0], best[1], best[2], rows)] = time_steps()
+        set_step_shape(sector, best[2], rows, best[3])
+        timings[(best[0], best[1], best[2], best[3], rows)] = time_steps()
     best = min(timings, key=timings.get)
     set_launch(sector, best[0], best[1])
-    set_step_shape(sector, best[2], best[3])
-    rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "rows_per_lane": best[2], "chunk_rows": best[3],
-           "ms_per_step": timings[best], "grid": get_launch(sector)[1],
-           "candidates": {f"{a},{b},{c},{d}": t for (a, b, c, d), t in timings.items()},
-           "candidate_key": "min_ctas_per_sm,ctas_per_sm,rows_per_lane,chunk_rows"}
+    set_step_shape(sector, best[2], best[4], best[3])
+    rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "rows_per_lane": best[2], "staged": best[3],
+           "chunk_rows": best[4], "ms_per_step": timings[best], "grid": get_launch(sector)[1],
+           "candidates": {",".join(str(v) for v in k): t for k, t in timings.items()},
+           "candidate_key": "min_ctas_per_sm,ctas_per_sm,rows_per_lane,staged,chunk_rows"}
     cache[key] = rec
     if use_cache:
         _save(cache)

@@ -148,15 +148,17 @@ int ed_sector_get_launch(const ed_sector* h, int* min_ctas_per_sm, int* grid) {
     return ED_OK;
 }
 
-int ed_sector_set_step_shape(ed_sector* h, int rows_per_lane, int chunk_rows) {
+int ed_sector_set_step_shape(ed_sector* h, int rows_per_lane, int chunk_rows, int staged_gathers) {
     if (!h) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: NULL sector");
-    return set_step_shape(h->s, rows_per_lane, chunk_rows);
+    return set_step_shape(h->s, rows_per_lane, chunk_rows, staged_gathers);
 }
 
-int ed_sector_get_step_shape(const ed_sector* h, int* rows_per_lane, int* chunk_rows) {
-    if (!h || !rows_per_lane || !chunk_rows) return set_error(ED_ERR_INVALID, "ed_sector_get_step_shape: NULL argument");
+int ed_sector_get_step_shape(const ed_sector* h, int* rows_per_lane, int* chunk_rows, int* staged_gathers) {
+    if (!h || !rows_per_lane || !chunk_rows || !staged_gathers)
+        return set_error(ED_ERR_INVALID, "ed_sector_get_step_shape: NULL argument");
     *rows_per_lane = h->s.seg_nr;
     *chunk_rows = h->s.seg_chunk_rows;
+    *staged_gathers = h->s.seg_staged;
     return ED_OK;
 }
 

@@ -434,7 +434,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
 
 // The fused H.v pass of one step over every row kind of a plan (device tables in `a`, whose idx
 // points at the whole kind-ordered id list), one launch per kind present.
-static int step_hv_all(int dtype, int minb, int nr, int free_grid, int other_grid, int cand_grid_f32,
+static int step_hv_all(int dtype, int minb, int nr, int staged, int free_grid, int other_grid, int cand_grid_f32,
                        const int kind_first[4], const int kind_count[4], StepArgs a, cudaStream_t st) {
     const int* idx0 = a.idx;
     // the expanded copies first: hops out of free blocks and the stabiliser rows read them
@@ -444,7 +444,7 @@ static int step_hv_all(int dtype, int minb, int nr, int free_grid, int other_gri
     a.idx = idx0 + kind_first[kRowsFree];
     a.count = kind_count[kRowsFree];
     a.grid = free_grid;
-    if (int rc = step_hv_free(dtype, minb, nr, a, st)) return rc;
+    if (int rc = step_hv_free(dtype, minb, nr, staged, a, st)) return rc;
     a.idx = idx0 + kind_first[kRowsCand];
     a.count = kind_count[kRowsCand];
     a.grid = dtype == ED_F32 ? cand_grid_f32 : other_grid;
@@ -470,7 +470,7 @@ namespace {
 struct BatchWorkspace {
     std::vector<uint64_t> serials;
     std::vector<int> chunk_rows;  // each sector's segment chunk length (its plan)
-    int device = -1, dtype = -1, m = 0, use_graph = 0, nr = 0;
+    int device = -1, dtype = -1, m = 0, use_graph = 0, nr = 0, staged = 0;
     HvWeights w{};
     int minb = 0, hv_grid = 0, other_grid = 0, cand_grid = 0;
     int nsec = 0, nchunks = 0, nhv = 0, ntasks = 0, stride = 0, grid = 0;
@@ -500,7 +500,8 @@ struct BatchWorkspace {
         for (int t = 0; t < 4; ++t)
             if (ww.w[t] != w.w[t]) return false;
         const Sector& s0 = *secs[0];
-        return ww.faithful == w.faithful && s0.hv_minb == minb && s0.seg_nr == nr && s0.hv_grid == hv_grid &&
+        return ww.faithful == w.faithful && s0.hv_minb == minb && s0.seg_nr == nr && s0.seg_staged == staged &&
+               s0.hv_grid == hv_grid &&
                s0.other_grid == other_grid && s0.cand_grid_f32 == cand_grid;
     }
 };
@@ -595,8 +596,8 @@ static int batch_steps(BatchWorkspace& W, const Sector& s0, const HvWeights& w, 
         void* other = b[(k + 1) % 2];
         StepArgs a{W.dviews.p, W.doffs.p, W.dhv.p, W.dkidx.p, 0, 0, W.smem, w, v, other, other, k == 0, W.coef.p,
                    W.stride, k, W.partials.p, W.dtasks.p, W.ntasks, (int64_t)s0.n_spin, W.xfull.p};
-        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.seg_nr, s0.hv_grid,
-                                 s0.other_grid, s0.cand_grid_f32, W.kind_first, W.kind_count, a, st))
+        if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s0.hv_minb, s0.seg_nr, s0.seg_staged,
+                                 s0.hv_grid, s0.other_grid, s0.cand_grid_f32, W.kind_first, W.kind_count, a, st))
             return rc;
         lanczos_scalars_kernel<<<W.nsec, kScalarThreads, 0, st>>>(W.partials.p, W.dhfirst.p, W.dhcount.p, W.coef.p,
                                                                   W.stride, k, 0, 0);
@@ -633,6 +634,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         W->w = w;
         W->minb = s0.hv_minb;
         W->nr = s0.seg_nr;
+        W->staged = s0.seg_staged;
         W->hv_grid = s0.hv_grid;
         W->other_grid = s0.other_grid;
         W->cand_grid = s0.cand_grid_f32;
@@ -769,8 +771,8 @@ static int single_hv_typed(const Sector& s, const HvWeights& w, const void* v, c
     StepArgs a{s.d_self.p, s.d_offs.p, s.d_hv_chunks.p, s.d_kidx.p, 0, 0, hv_smem_bytes(s.view, sizeof(R)), w,
                const_cast<void*>(v), const_cast<void*>(vprev), vnext, vprev == nullptr, scal, 0, 0, s.d_partials.p,
                s.d_tasks.p, s.n_tasks, (int64_t)s.n_spin, s.d_xfull.p};
-    if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.seg_nr, s.hv_grid, s.other_grid,
-                             s.cand_grid_f32, s.kind_first, s.kind_count, a, st))
+    if (int rc = step_hv_all(dtype_code(sizeof(R) == 8, CPLX), s.hv_minb, s.seg_nr, s.seg_staged, s.hv_grid,
+                             s.other_grid, s.cand_grid_f32, s.kind_first, s.kind_count, a, st))
         return rc;
     lanczos_scalars_kernel<<<1, kScalarThreads, 0, st>>>(s.d_partials.p, s.d_hv_first.p, s.d_hv_count.p, scal, 0, 0, 0,
                                                          0);
@@ -793,14 +795,16 @@ int set_launch(Sector& s, int minb, int ctas_per_sm) {
     return ED_OK;
 }
 
-// Rows per lane of the free-row kernel (1, 2, or 0 = by dtype) and the rows of a segment chunk (a power
-// of two from 1024 to 65536).  A new chunk length re-plans the sector's steps: its per-chunk sums,
+// Rows per lane of the free-row kernel (1, 2, or 0 = by dtype), the rows of a segment chunk (a power of
+// two from 1024 to 65536) and whether its gathers go through shared memory.  A new chunk length re-plans the sector's steps: its per-chunk sums,
 // and with them the last bits of its recursions, follow the plan (the same alone and in a batch).
-int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows) {
+int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows, int staged) {
     if (rows_per_lane < 0 || rows_per_lane > 2) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: rows per lane");
+    if (staged != 0 && staged != 1) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: staged must be 0 or 1");
     if (chunk_rows < 1024 || chunk_rows > 65536 || (chunk_rows & (chunk_rows - 1)))
         return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: chunk rows must be a power of two in [1024, 65536]");
     s.seg_nr = rows_per_lane;
+    s.seg_staged = staged;
     if (chunk_rows == s.seg_chunk_rows) return ED_OK;
     s.seg_chunk_rows = chunk_rows;
     return s.built ? single_setup(s) : ED_OK;

@@ -137,6 +137,7 @@ struct Sector {
     int hv_grid = 0;             // persistent grid of the H.v kernels (free-row step kernel)
     int hv_minb = 3;             // launch variant of the free-row step kernel (minimum resident CTAs per SM)
     int seg_nr = 0;              // rows per lane the free-row kernel works on together (0: by dtype)
+    int seg_staged = 0;          // 1: the free-row kernel gathers through shared memory (cp.async)
     int seg_chunk_rows = kSegChunkRows;  // rows of a segment chunk (the plan's unit of work and of partial sums)
     int other_grid = 0;          // grid of the other row kinds' step kernels
     int cand_grid_f32 = 0;       // grid of the stabiliser-row kernel for real FP32 vectors
@@ -244,7 +245,7 @@ int single_setup(Sector& s);
 int build_descriptors(Sector& s);
 int seg_records_build(Sector& s, const std::vector<int>& free_blocks, int64_t nseg);  // ed_segrec.cu
 int set_launch(Sector& s, int minb, int ctas_per_sm);
-int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows);  // re-plans when chunk_rows changes
+int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows, int staged);  // re-plans when chunk_rows changes
 void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& plan);
 
 // ed_step_free.cu / ed_step_rest.cu: the fused step kernel of one row kind over a list of chunks
@@ -271,7 +272,8 @@ struct StepArgs {
     int64_t n_spin;
     void* xfull;
 };
-int step_hv_free(int dtype, int minb, int nr, const StepArgs& a, cudaStream_t st);
+int step_hv_free(int dtype, int minb, int nr, int staged, const StepArgs& a, cudaStream_t st);
+int step_hv_free_staged(int dtype, int nr, const StepArgs& a, cudaStream_t st);
 int step_hv_free_nr1(int dtype, int minb, const StepArgs& a, cudaStream_t st);
 int step_hv_free_split(int dtype, int nr, const StepArgs& a, cudaStream_t st);
 // rows per lane of the free-row kernel for a dtype when the sector leaves it open (seg_nr = 0)

@@ -133,6 +133,30 @@ __device__ __forceinline__ void seg_ld(const typename Vec<R, CPLX>::T* p, R& re,
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
 
+// Adds a hop's term c * v to a row's hop sum (c, v complex when CPLX), by explicit fused
+// multiply-adds so that every path of the kernel rounds it the same way.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void seg_hop_acc(R& hr, R& hi, R cr, R ci, R vr, R vi) {
+    hr = fma_r(cr, vr, hr);
+    if constexpr (CPLX) {
+        hr = fma_r(-ci, vi, hr);
+        hi = fma_r(ci, vr, fma_r(cr, vi, hi));
+    }
+}
+
+template <typename R, bool CPLX>
+__device__ __forceinline__ void seg_ld_shared(const typename Vec<R, CPLX>::T* p, R& re, R& im) {
+    const typename Vec<R, CPLX>::T t = *p;
+    if constexpr (CPLX) {
+        re = t.x;
+        im = t.y;
+    } else {
+        re = t;
+        im = R(0);
+    }
+}
+
+
 template <typename R>
 __device__ __forceinline__ void fold(Accum<R>& a, R p);
 template <>
@@ -170,6 +194,18 @@ __device__ __forceinline__ void seg_add(R& er, R& ei, R& lr, R& li, bool rung, R
     }
 }
 
+// Copies one vector element global -> shared asynchronously (cp.async; 4, 8 or 16 bytes).
+template <typename T>
+__device__ __forceinline__ void seg_cp_async_elem(T* smem_dst, const T* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    if constexpr (sizeof(T) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(gsrc), "n"((int)sizeof(T)) : "memory");
+}
+
+constexpr int kSegStageBytes = 10240;  // staged gathers: shared memory per warp
+
 constexpr int kSegLowMax = 16;  // antiparallel bonds below P of one row (at most kSegMaxA), padded to fours
 
 // A hop slot of a chunk as every row reads it: the target values, the coefficient, the slot's first
@@ -187,13 +223,19 @@ struct alignas(16) SegSlot<R, true> {
     uint32_t off;
 };
 
+template <typename R, bool CPLX>
+__device__ __forceinline__ R seg_slot_ci(const SegSlot<R, CPLX>& S) {
+    if constexpr (CPLX) return S.ci;
+    else return R(0);
+}
+
 // The fused step over segment chunks: a chunk is (free block, class kl, 64-offset window, range of
 // segments); warp w of the CTA takes segments begin + w, begin + w + 8, ... and, in each, the rows at
 // offsets t = window + lane and t + 32.  NR rows are worked on together (their gathers in flight
 // at once, the segment's record words read once for both); NR = 1 takes the two rows one after
 // the other.  MERGED: rung and leg exchanges share one coefficient (J_rung = J_leg), so each row keeps
 // one exchange sum over one list per bond class; otherwise every element picks its coefficient.
-template <typename R, bool CPLX, int MINB, bool MERGED, int NR>
+template <typename R, bool CPLX, int MINB, bool MERGED, int NR, bool STAGED = false>
 __global__ void __launch_bounds__(kSegThreads, MINB)
     seg_step_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                     const BatchChunk* __restrict__ chunks, const int* __restrict__ idx, int count, HvWeights W,
@@ -201,6 +243,9 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     double* __restrict__ partials, void* xfull) {
     using T = typename Vec<R, CPLX>::T;
     constexpr int kWarps = kSegThreads / 32;
+    constexpr int kCols = 32 * NR;  // staged gathers: columns of a slot (the rows worked on together)
+    constexpr int kScap = kSegStageBytes / (kCols * (int)sizeof(T));  // staged slots per pass
+    extern __shared__ __align__(16) uint8_t seg_stage_smem[];  // STAGED: kWarps * kSegStageBytes
     __shared__ uint8_t s_rt[kSegLow];           // rank_P of each P-bit mask within its popcount class
     __shared__ uint16_t s_ut[kSegLow];          // the masks by (popcount, rank_P)
     __shared__ uint32_t s_utoff[kSegA + 2];
@@ -457,100 +502,160 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     xm[r] = ((lnw[h0 + r] >> 16) ^ hib) & xall;
                     er[r] = ei[r] = lr[r] = li[r] = hr[r] = hi[r] = R(0);
                 }
-                // exchange bonds below P: partners in the same segment, four loads at a time per row
-                for (int q0 = 0; q0 < smax; q0 += 4) {
-                    R vr[NR][4], vi[NR][4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r)
-                            seg_ld<R, CPLX>(xs + (uint32_t)s_al[q0 + u][lane + 32 * (h0 + r)], vr[r][u], vi[r][u]);
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < (int)(cnt[h0 + r] & 255u), vr[r][u], vi[r][u]);
-                }
-                // exchange bonds at or above P: the partner segments at the same offsets, four at a time
-                for (int q0 = 0; q0 < zb4; q0 += 4) {
-                    R vr[NR][4], vi[NR][4];
-                    const uint4 pw = *reinterpret_cast<const uint4*>(sw + 4 + q0);  // 16-byte aligned
-                    const uint32_t pq[4] = {pw.x, pw.y, pw.z, pw.w};
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xt[r] + pq[u], vr[r][u], vi[r][u]);
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr, vr[r][u], vi[r][u]);
-                }
-                // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
-                for (int c0 = 0; c0 < nX4; c0 += 4) {
-                    R vr[NR][4], vi[NR][4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int cc = c0 + u;
-                        const uint32_t pw = sw[xo + cc];
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) {
-                            const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
-                            const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
-                                               (~on & (base + (uint32_t)tt[h0 + r]));
-                            seg_ld<R, CPLX>(xb + o, vr[r][u], vi[r][u]);
-                        }
+                if constexpr (!STAGED) {
+                    // exchange bonds below P: partners in the same segment, four loads at a time per row
+                    for (int q0 = 0; q0 < smax; q0 += 4) {
+                        R vr[NR][4], vi[NR][4];
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                seg_ld<R, CPLX>(xs + (uint32_t)s_al[q0 + u][lane + 32 * (h0 + r)], vr[r][u], vi[r][u]);
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < (int)(cnt[h0 + r] & 255u), vr[r][u], vi[r][u]);
                     }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], c0 + u < nXr, vr[r][u], vi[r][u]);
-                }
-                // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
-                for (int h4 = 0; h4 < n04; h4 += 4) {
-                    R vr[NR][4], vi[NR][4];
-                    SegSlot<R, CPLX> S[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        S[u] = s_slot[h4 + u];
-                        const uint32_t sb = sw[S[u].off];
-#pragma unroll
-                        for (int r = 0; r < NR; ++r)
-                            seg_ld<R, CPLX>(S[u].tp + (sb + s_hc[h4 + u][lane + 32 * (h0 + r)]), vr[r][u], vi[r][u]);
+                    // exchange bonds at or above P: the partner segments at the same offsets, four at a time
+                    for (int q0 = 0; q0 < zb4; q0 += 4) {
+                        R vr[NR][4], vi[NR][4];
+                        const uint4 pw = *reinterpret_cast<const uint4*>(sw + 4 + q0);  // 16-byte aligned
+                        const uint32_t pq[4] = {pw.x, pw.y, pw.z, pw.w};
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xt[r] + pq[u], vr[r][u], vi[r][u]);
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr, vr[r][u], vi[r][u]);
                     }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) {
-                            hr[r] += S[u].cr * vr[r][u];
-                            if constexpr (CPLX) {
-                                hr[r] -= S[u].ci * vi[r][u];
-                                hi[r] += S[u].cr * vi[r][u] + S[u].ci * vr[r][u];
+                    // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
+                    for (int c0 = 0; c0 < nX4; c0 += 4) {
+                        R vr[NR][4], vi[NR][4];
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int cc = c0 + u;
+                            const uint32_t pw = sw[xo + cc];
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
+                                const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
+                                                   (~on & (base + (uint32_t)tt[h0 + r]));
+                                seg_ld<R, CPLX>(xb + o, vr[r][u], vi[r][u]);
                             }
                         }
-                }
-                for (int h4 = n04; h4 < n04 + n124; h4 += 4) {
-                    R vr[NR][4], vi[NR][4];
-                    SegSlot<R, CPLX> S[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        S[u] = s_slot[h4 + u];
-                        const uint32_t ua = sw[S[u].off];
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) {
-                            const uint32_t hc = s_hc[h4 + u][lane + 32 * (h0 + r)];
-                            const uint32_t rr = sw[S[u].off + 1u + (hc >> kSegA)] + s_rt[ua | (hc & (kSegLow - 1u))];
-                            seg_ld<R, CPLX>(S[u].tp + rr, vr[r][u], vi[r][u]);
-                        }
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], c0 + u < nXr, vr[r][u], vi[r][u]);
                     }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int r = 0; r < NR; ++r) {
-                            hr[r] += S[u].cr * vr[r][u];
-                            if constexpr (CPLX) {
-                                hr[r] -= S[u].ci * vi[r][u];
-                                hi[r] += S[u].cr * vi[r][u] + S[u].ci * vr[r][u];
+                    // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
+                    for (int h4 = 0; h4 < n04; h4 += 4) {
+                        R vr[NR][4], vi[NR][4];
+                        SegSlot<R, CPLX> S[4];
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            S[u] = s_slot[h4 + u];
+                            const uint32_t sb = sw[S[u].off];
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                seg_ld<R, CPLX>(S[u].tp + (sb + s_hc[h4 + u][lane + 32 * (h0 + r)]), vr[r][u], vi[r][u]);
+                        }
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                seg_hop_acc<R, CPLX>(hr[r], hi[r], S[u].cr, seg_slot_ci(S[u]), vr[r][u], vi[r][u]);
+                            }
+                    }
+                    for (int h4 = n04; h4 < n04 + n124; h4 += 4) {
+                        R vr[NR][4], vi[NR][4];
+                        SegSlot<R, CPLX> S[4];
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            S[u] = s_slot[h4 + u];
+                            const uint32_t ua = sw[S[u].off];
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                const uint32_t hc = s_hc[h4 + u][lane + 32 * (h0 + r)];
+                                const uint32_t rr = sw[S[u].off + 1u + (hc >> kSegA)] + s_rt[ua | (hc & (kSegLow - 1u))];
+                                seg_ld<R, CPLX>(S[u].tp + rr, vr[r][u], vi[r][u]);
                             }
                         }
+    #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+    #pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                seg_hop_acc<R, CPLX>(hr[r], hi[r], S[u].cr, seg_slot_ci(S[u]), vr[r][u], vi[r][u]);
+                            }
+                    }
+                } else {
+                    // every gather of the rows goes to shared memory by cp.async, up to kScap slots per
+                    // pass: all in flight together, one wait, then the sums read them back.  Slots:
+                    // low bonds [0, e0), high [e0, e1), cross [e1, e2), hop slots [e2, e3)
+                    T* const stg = reinterpret_cast<T*>(seg_stage_smem) + (size_t)warp * kScap * kCols;
+                    const int e0 = smax, e1 = e0 + zb4, e2 = e1 + nX4, e3 = e2 + n04 + n124;
+                    for (int p0 = 0; p0 < e3; p0 += kScap) {
+                        const int p1 = min(e3, p0 + kScap);
+                        for (int sl = p0; sl < min(p1, e0); ++sl)
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r,
+                                                     xs + (uint32_t)s_al[sl][lane + 32 * (h0 + r)]);
+                        for (int sl = max(p0, e0); sl < min(p1, e1); ++sl) {
+                            const uint32_t pw = sw[4 + sl - e0];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xt[r] + pw);
+                        }
+                        for (int sl = max(p0, e1); sl < min(p1, e2); ++sl) {
+                            const int cc = sl - e1;
+                            const uint32_t pw = sw[xo + cc];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
+                                const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
+                                                   (~on & (base + (uint32_t)tt[h0 + r]));
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xb + o);
+                            }
+                        }
+                        for (int sl = max(p0, e2); sl < p1; ++sl) {
+                            const int hs = sl - e2;  // hop slot: kind 0 below n04, kind 1 from n04
+                            const SegSlot<R, CPLX>& S = s_slot[hs];
+                            const uint32_t w0 = sw[S.off];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                const uint32_t hc = s_hc[hs][lane + 32 * (h0 + r)];
+                                const uint32_t rr = hs < n04 ? w0 + hc
+                                                             : sw[S.off + 1u + (hc >> kSegA)] +
+                                                                   s_rt[w0 | (hc & (kSegLow - 1u))];
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, S.tp + rr);
+                            }
+                        }
+                        seg_cp_commit();
+                        seg_cp_wait<0>();
+                        __syncwarp(__activemask());
+                        for (int sl = p0; sl < min(p1, e2); ++sl)
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                R vr, vi;
+                                seg_ld_shared<R, CPLX>(stg + (sl - p0) * kCols + lane + 32 * r, vr, vi);
+                                const bool rung = sl < e0 ? sl < (int)(cnt[h0 + r] & 255u)
+                                                          : (sl < e1 ? sl - e0 < zbr : sl - e1 < nXr);
+                                seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], rung, vr, vi);
+                            }
+                        for (int sl = max(p0, e2); sl < p1; ++sl) {
+                            const SegSlot<R, CPLX>& S = s_slot[sl - e2];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) {
+                                R vr, vi;
+                                seg_ld_shared<R, CPLX>(stg + (sl - p0) * kCols + lane + 32 * r, vr, vi);
+                                seg_hop_acc<R, CPLX>(hr[r], hi[r], S.cr, seg_slot_ci(S), vr, vi);
+                            }
+                        }
+                        __syncwarp(__activemask());  // the pass's slots are read before the next pass writes them
+                    }
                 }
                 if (n0 + n12 < nhop) {
                     // hops that move more than two low positions above P: the full rank of U | V
@@ -565,11 +670,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                             const uint32_t rr = spin_rank(sw[s_desc.hop_off[hh]] | V, RT, Nd);
                             R vr, vi;
                             seg_ld<R, CPLX>(F.tp + rr, vr, vi);
-                            hr[r] += F.cr * vr;
-                            if constexpr (CPLX) {
-                                hr[r] -= F.ci * vi;
-                                hi[r] += F.cr * vi + F.ci * vr;
-                            }
+                            seg_hop_acc<R, CPLX>(hr[r], hi[r], F.cr, F.ci, vr, vi);
                         }
                     }
                 }

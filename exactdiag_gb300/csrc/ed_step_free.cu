@@ -42,8 +42,9 @@ int seg_occupancy() {
 
 }  // namespace
 
-int step_hv_free(int dtype, int minb, int nr, const StepArgs& a, cudaStream_t st) {
+int step_hv_free(int dtype, int minb, int nr, int staged, const StepArgs& a, cudaStream_t st) {
     nr = seg_rows_for(dtype, nr);
+    if (staged) return step_hv_free_staged(dtype, nr, a, st);
     // one exchange coefficient when J_rung = J_leg (the sums need no per-element choice)
     if (a.w.w[2] != a.w.w[3]) return step_hv_free_split(dtype, nr, a, st);
     if (nr == 1) return step_hv_free_nr1(dtype, minb, a, st);

@@ -67,9 +67,11 @@ int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
  * chunk_rows, the rows of one chunk of work (a power of two in [1024, 65536]; default 16384).  The
  * rows per lane do not change results; a new chunk length re-plans the sector, and since the step's
  * partial sums are kept per chunk, its recursions then differ in the last bits (a sector still gives
- * the same bits alone and in a batch).  ED_ERR_INVALID for values out of range. */
-int ed_sector_set_step_shape(ed_sector* s, int rows_per_lane, int chunk_rows);
-int ed_sector_get_step_shape(const ed_sector* s, int* rows_per_lane, int* chunk_rows);
+ * the same bits alone and in a batch).  staged_gathers = 1 sends the free-row kernel's gathers through
+ * shared memory (cp.async; results unchanged, at most two CTAs per SM).  ED_ERR_INVALID for values out
+ * of range. */
+int ed_sector_set_step_shape(ed_sector* s, int rows_per_lane, int chunk_rows, int staged_gathers);
+int ed_sector_get_step_shape(const ed_sector* s, int* rows_per_lane, int* chunk_rows, int* staged_gathers);
 
 /* Chunks of the sector's fused step per row kind: counts[0] chunks of rows of blocks with a
  * trivial stabiliser (colex-delta rows), counts[1] chunks of rows of blocks with a small

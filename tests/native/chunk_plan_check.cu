@@ -15,7 +15,7 @@ namespace ed {
 // the other translation units of the library, not exercised here
 int set_error(int code, const char*) { return code; }
 int set_cuda_error(cudaError_t, const char*) { return ED_ERR_CUDA; }
-int step_hv_free(int, int, int, const StepArgs&, cudaStream_t) { return 0; }
+int step_hv_free(int, int, int, int, const StepArgs&, cudaStream_t) { return 0; }
 int step_expand(int, const StepArgs&, cudaStream_t) { return 0; }
 int step_hv_cand(int, const StepArgs&, cudaStream_t) { return 0; }
 int step_hv_generic(int, const StepArgs&, cudaStream_t) { return 0; }

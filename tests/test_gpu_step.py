@@ -106,21 +106,23 @@ def test_step_shapes(cuda, key, precision):
         return y, scal[:4].cpu().numpy()
 
     first_y, first_s = step()
-    for minb, ctas in autotune.CANDIDATES:
-        for nr in (1, 2):
-            autotune.set_launch(sec, minb, ctas)
-            autotune.set_step_shape(sec, nr, autotune.DEFAULT_CHUNK_ROWS)
-            y, s = step()
-            assert torch.equal(y, first_y) and np.array_equal(s, first_s), (minb, ctas, nr)
+    shapes = [(minb, ctas, nr, 0) for minb, ctas in autotune.CANDIDATES for nr in (1, 2)]
+    shapes += [(minb, ctas, nr, 1) for minb, ctas, nr in autotune.STAGED_CANDIDATES]
+    for minb, ctas, nr, staged in shapes:
+        autotune.set_launch(sec, minb, ctas)
+        autotune.set_step_shape(sec, nr, autotune.DEFAULT_CHUNK_ROWS, staged)
+        y, s = step()
+        assert torch.equal(y, first_y) and np.array_equal(s, first_s), (minb, ctas, nr, staged)
+    autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS, 0)
     for rows in (1024, 4096, 8192, 32768, 65536):
         autotune.set_step_shape(sec, 0, rows)
-        assert autotune.get_step_shape(sec) == (0, rows)
+        assert autotune.get_step_shape(sec) == (0, rows, 0)
         y, s = step()
         assert float(torch.max(torch.abs(y - ref)).item()) <= tol * scale, rows
         assert abs(s[1] - first_s[1]) <= 1e-9 * max(1.0, abs(first_s[1])) * (1 if precision == "fp64" else 1e3)
     autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS)
     y, s = step()
     assert torch.equal(y, first_y) and np.array_equal(s, first_s)
-    for bad in ((3, 16384), (-1, 16384), (1, 12288), (1, 512), (2, 131072)):
+    for bad in ((3, 16384, 0), (-1, 16384, 0), (1, 12288, 0), (1, 512, 0), (2, 131072, 0), (1, 16384, 2)):
         with pytest.raises(nat.EngineError):
             autotune.set_step_shape(sec, *bad)

@@ -106,38 +106,45 @@ def _lowest_ritz(a: np.ndarray, b_next: np.ndarray):
 class CheckedLanczos:
     """A ground-state Lanczos recursion that reads its coefficients every `check_every` steps and
     stops once the lowest Ritz value changes by at most `tol` (relative) over a window, on breakdown,
-    or after `max_steps`.  With `store`, every Lanczos vector is kept (one extra vector of the run's
-    dtype per step) so that the Ritz vector needs no second pass; otherwise two buffers rotate."""
+    or after `max_steps`.  The first `keep` Lanczos vectors are kept (one vector of the run's dtype
+    each) and the later ones rotate over two buffers; the Ritz vector then takes the kept vectors as
+    they are and regenerates only the others, by continuing the recursion from the last two kept ones
+    (the fused step is deterministic, so the regenerated vectors are the same bits)."""
 
-    def __init__(self, sector: DeviceSector, weights, dtype: torch.dtype, max_steps: int, store: bool):
+    def __init__(self, sector: DeviceSector, weights, dtype: torch.dtype, max_steps: int, keep: int = 0):
         from exactdiag_gb300 import autotune
 
         self.sector, self.weights, self.dtype = sector, weights_tuple(weights), dtype
         self.max_steps = int(max_steps)
-        self.store = store
+        self.keep = max(0, min(int(keep), self.max_steps + 1))
         dev = sector.device
         # kept vectors are allocated as the recursion reaches them
-        self.V = [torch.zeros(sector.n, dtype=dtype, device=dev) for _ in range(2)]
+        self.V: list[torch.Tensor] = []
+        self.R = [torch.zeros(sector.n, dtype=dtype, device=dev) for _ in range(2)]
         self.scal = torch.zeros(2 * self.max_steps + 4, dtype=torch.float64, device=dev)
         self.norm = torch.zeros(1, dtype=torch.float64, device=dev)
         autotune.ensure(sector, self.weights, dtype)
 
     def _buf(self, k: int) -> torch.Tensor:
-        if not self.store:
-            return self.V[k % 2]
-        while len(self.V) <= k:
-            self.V.append(torch.empty_like(self.V[0]))
-        return self.V[k]
+        if k < self.keep:
+            while len(self.V) <= k:
+                self.V.append(torch.empty_like(self.R[0]))
+            return self.V[k]
+        return self.R[(k - self.keep) % 2]
+
+    def _step(self, k: int, scal: torch.Tensor) -> None:
+        # v_{k+1} overwrites v_{k-1} in place once both rotate; before that they are distinct buffers
+        self.sector.lanczos_step(self.weights, self._buf(k), self._buf(k - 1) if k > 0 else None,
+                                 self._buf(k + 1), scal[2 * k: 2 * k + 4])
 
     def run(self, v0: torch.Tensor, tol: float, check_every: int = 10, min_steps: int = 2) -> dict:
         s = self.sector
-        self.V[0].copy_(v0)
-        s.normalize(self.V[0], self.norm)
+        self._buf(0).copy_(v0)
+        s.normalize(self._buf(0), self.norm)
         self.scal.zero_()
         theta_prev, steps = None, self.max_steps
         for k in range(self.max_steps):
-            v, nxt = self._buf(k), self._buf(k + 1)
-            s.lanczos_step(self.weights, v, self._buf(k - 1) if k > 0 else None, nxt, self.scal[2 * k: 2 * k + 4])
+            self._step(k, self.scal)
             m = k + 1
             if m % check_every and m != self.max_steps:
                 continue
@@ -160,22 +167,31 @@ class CheckedLanczos:
         return {"theta": self.theta, "steps": steps, "residual": self.residual}
 
     def ritz_vector(self, v0: torch.Tensor) -> torch.Tensor:
-        """The lowest Ritz vector in FP64 (complex128 for complex sectors): from the stored vectors,
-        else by a second, bitwise-identical pass from v0."""
+        """The lowest Ritz vector in FP64 (complex128 for complex sectors): the kept vectors as they
+        are, the others regenerated (from v0 when none is kept)."""
         s = self.sector
         acc = torch.zeros(s.n, dtype=torch.float64 if s.is_real else torch.complex128, device=s.device)
-        if self.store:
-            for k in range(self.steps):
-                s.accumulate(self.V[k], complex(self.s[k]), acc)
+        kept = min(self.keep, self.steps)
+        if kept < 2 and kept < self.steps:
+            kept = 0  # too few kept to continue from: regenerate from v0
+        for k in range(kept):
+            s.accumulate(self.V[k], complex(self.s[k]), acc)
+        if kept == self.steps:
             return acc
-        self.V[0].copy_(v0)
-        s.normalize(self.V[0], self.norm)
-        scal = torch.zeros_like(self.scal)
-        for k in range(self.steps):
-            v, nxt = self._buf(k), self._buf(k + 1)
-            s.accumulate(v, complex(self.s[k]), acc)
-            if k + 1 < self.steps:
-                s.lanczos_step(self.weights, v, self._buf(k - 1) if k > 0 else None, nxt, scal[2 * k: 2 * k + 4])
+        if kept >= 2:
+            # continue from v_{kept-2}, v_{kept-1}: step kept-1 writes v_kept again, and so on; the
+            # scalars it reads (b_k) are the first pass's, the ones it writes the same bits
+            start = kept - 1
+        else:
+            self.keep = 0
+            self.V.clear()
+            self._buf(0).copy_(v0)
+            s.normalize(self._buf(0), self.norm)
+            s.accumulate(self._buf(0), complex(self.s[0]), acc)
+            start = 0
+        for k in range(start, self.steps - 1):
+            self._step(k, self.scal)
+            s.accumulate(self._buf(k + 1), complex(self.s[k + 1]), acc)
         return acc
 
 
@@ -190,15 +206,16 @@ def _vectors_that_fit(sector: DeviceSector, dtype: torch.dtype, fraction: float 
 
 def ground_state(sector: DeviceSector, weights, max_steps: int = 240, precision: str = "mixed", seed: int = 0,
                  v0: torch.Tensor | None = None, tol: float = 1e-13, fp32_tol: float = 1e-7,
-                 refine_max: int = 160, check_every: int = 10, store: bool | None = None) -> dict:
+                 refine_max: int = 160, check_every: int = 10, keep_vectors: int | None = None) -> dict:
     """Ground energy of a sector, each form run until its lowest Ritz value has converged.
 
     precision "fp64": plain FP64 Lanczos until the lowest Ritz value changes by at most `tol`
     (relative) over `check_every` steps.
     precision "mixed": FP32 (complex64) Lanczos with FP64 reductions until the Ritz value changes by
     at most `fp32_tol` (the FP32 vectors' resolution); the Ritz vector is accumulated in FP64 from the
-    kept FP32 Lanczos vectors (a second pass when they do not fit in device memory) and refined by
-    FP64 Lanczos started from it, until its Ritz value changes by at most `tol`.  E0 is the refined
+    FP32 Lanczos vectors -- those kept in device memory as they are (`keep_vectors`, by default as many
+    as fit), the others regenerated by a second pass from the last two kept -- and refined by FP64
+    Lanczos started from it, until its Ritz value changes by at most `tol`.  E0 is the refined
     value; the result also carries the step counts and the wall time of each phase.
     """
     import time
@@ -212,33 +229,36 @@ def ground_state(sector: DeviceSector, weights, max_steps: int = 240, precision:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     if precision == "fp64":
-        run = CheckedLanczos(sector, weights, dt, max_steps, store=False)
+        run = CheckedLanczos(sector, weights, dt, max_steps)
         r = run.run(v0, tol, check_every)
         torch.cuda.synchronize()
         return {"E0": r["theta"], "theta": r["theta"], "steps": r["steps"], "residual": r["residual"],
                 "a": run.a, "time_s": time.perf_counter() - t0}
     steps32 = max_steps
-    if store is None:
-        # keep the FP32 vectors when at least 100 of them fit; the FP32 stage then stops where they run
-        # out at the latest (the refinement takes the rest of the convergence)
-        cap = _vectors_that_fit(sector, dt) - 1
-        keep = cap >= 100
-        if keep:
+    cap = _vectors_that_fit(sector, dt) - 2  # two more buffers rotate beside the kept vectors
+    if keep_vectors is None:
+        # keep every FP32 vector when at least 100 fit (the FP32 stage then stops where they run out
+        # at the latest; the refinement takes the rest of the convergence); else keep as many as fit
+        # and regenerate the others for the Ritz vector
+        if cap >= 100:
             steps32 = min(max_steps, cap)
+            keep = steps32 + 1
+        else:
+            keep = max(0, cap)
     else:
-        keep = store
-    run = CheckedLanczos(sector, weights, dt, steps32, store=keep)
+        keep = int(keep_vectors)
+    run = CheckedLanczos(sector, weights, dt, steps32, keep=keep)
     r = run.run(v0, fp32_tol, check_every)
     psi = run.ritz_vector(v0)
     del run
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    ref = CheckedLanczos(sector, weights, psi.dtype, refine_max, store=False)
+    ref = CheckedLanczos(sector, weights, psi.dtype, refine_max)
     rr = ref.run(psi, tol, check_every=4)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     return {"E0": rr["theta"], "theta": r["theta"], "steps": r["steps"], "refine_steps": rr["steps"],
-            "residual": rr["residual"], "rayleigh": float(ref.a[0]), "kept_vectors": keep,
+            "residual": rr["residual"], "rayleigh": float(ref.a[0]), "kept_vectors": min(keep, r["steps"]),
             "time_s": t2 - t0, "time_fp32_s": t1 - t0, "time_refine_s": t2 - t1}
 
 

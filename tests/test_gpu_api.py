@@ -334,3 +334,22 @@ def test_doped_spectral_functions_plus_and_minus_batched_equals_sequential(torch
     shutil.rmtree(in_tmp / "calculations")
     ws_s, sp_s, _ = api.get_spectral_function_spectra(cfg, limited_qs=True, batched=False)
     assert np.max(np.abs(sp_b - sp_s)) == 0.0
+
+
+@pytest.mark.parametrize("key", [(8, 2, 7, 0, 0), (8, 2, 7, 3, 1)])
+def test_mixed_ground_state_kept_and_regenerated_vectors_agree(torch, oracle, key):
+    """The mixed ground state's Ritz vector is the same bits whether every FP32 Lanczos vector is
+    kept, only the first few (the rest regenerated from the last two kept), or none (a second pass
+    from the start vector); its refined energy matches the oracle's lowest eigenvalue."""
+    from exactdiag_gb300.lanczos import ground_state
+
+    sec = _sector(key)
+    sec_o = oracle.Sector(*key)
+    bas = oracle.basis(sec_o)
+    want = oracle.lowest_eigvals(oracle.hamiltonian(sec_o, W, bas), 1)[0]
+    runs = [ground_state(sec, W, 120, precision="mixed", seed=3, keep_vectors=k) for k in (1000, 7, 0)]
+    for g in runs:
+        assert abs(g["E0"] - want) <= 1e-10 * abs(want), (g["E0"], want)
+        assert g["steps"] == runs[0]["steps"] and g["refine_steps"] == runs[0]["refine_steps"]
+    assert runs[0]["E0"] == runs[1]["E0"] == runs[2]["E0"]
+    assert runs[0]["kept_vectors"] == runs[0]["steps"] and runs[1]["kept_vectors"] == 7 and runs[2]["kept_vectors"] == 0

@@ -288,10 +288,6 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     const R wr = R(0.5) * (R)W.w[3], wl = R(0.5) * (R)W.w[2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // the chunk whose tables the shared memory holds: a CTA's next chunk of the same (sector, block,
-    // class, window) keeps them (with the grid a multiple of the windows of a range, a CTA's chunks
-    // share their window and mostly their block and class)
-    int held_sec = -1, held_block = -1, held_kl = -1, held_piece = -1;
     for (int c = blockIdx.x; c < count; c += gridDim.x) {
         const int cid = idx[c];
         const BatchChunk ch = chunks[cid];
@@ -301,23 +297,18 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int nA = (int)comb[kl * kCombStride + P];
         const int win = kSegWin * ch.piece;
         const int nact = min(32, nA - win);  // lanes with a first row
-        const bool held = ch.sec == held_sec && ch.block == held_block && kl == held_kl && ch.piece == held_piece;
-        held_sec = ch.sec;
-        held_block = ch.block;
-        held_kl = kl;
-        held_piece = ch.piece;
         __syncthreads();  // the previous chunk's rows are done with the shared tables
-        if (!held) {
+        {
             const uint4* src = reinterpret_cast<const uint4*>(Sp->seg + ch.block);
             uint4* dst = reinterpret_cast<uint4*>(&s_desc);
             for (int i = threadIdx.x; i < (int)(sizeof(SegDesc) / 16); i += blockDim.x) dst[i] = src[i];
-            __syncthreads();
         }
+        __syncthreads();
         const int nhop = s_desc.nhop, n0 = s_desc.n0, n12 = s_desc.n12, nX = s_desc.nX, nXr = s_desc.nXr;
         const int64_t bstart = s_desc.start;
         T* const x = reinterpret_cast<T*>(v) + offs[ch.sec];
         const T* const xb = x + bstart;
-        if (!held) {  // the chunk's tables: hop records, per-offset terms, hop slots
+        {  // the chunk's tables: hop records, per-offset terms, hop slots
             if (warp == 2 && lane < kMaxHops) {
                 // every hop gets a record: absent hops (and those past nhop) read a valid element with
                 // coefficient 0

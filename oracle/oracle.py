@@ -257,6 +257,17 @@ def excitation_matrix(sec: Sector, bas, name: str, qx: int, qy: int, fsec: Secto
     return _csc(colptr, rows, vals, (len(fbas[0]), len(bas[0]))).tocsr()
 
 
+def _start_vector(n: int, dtype) -> np.ndarray:
+    """Seeded random start vector for eigsh.  A uniform one is not safe: it can lie in a subspace
+    of a residual symmetry of the sector and miss the ground state there (2x8, two holes,
+    k = (3, 1): all ones finds -9.7705, the second level, not the ground state -9.8664)."""
+    rng = np.random.default_rng(1234)
+    v = rng.uniform(-1, 1, n)
+    if np.iscomplexobj(np.zeros(0, dtype)):
+        v = v + 1j * rng.uniform(-1, 1, n)
+    return (v / np.linalg.norm(v)).astype(dtype)
+
+
 def lowest_eigvals(h, k: int, tol: float = 1e-14):
     """Tight FP64 eigen-oracle: dense eigh for small n, eigsh otherwise."""
     n = h.shape[0]
@@ -266,7 +277,7 @@ def lowest_eigvals(h, k: int, tol: float = 1e-14):
         return np.sort(np.linalg.eigvalsh(h.toarray()))[:k]
     import scipy.sparse.linalg as spl
 
-    vals = spl.eigsh(h, k=min(k, n - 2), which="SA", tol=tol, v0=np.ones(n, h.dtype) / np.sqrt(n),
+    vals = spl.eigsh(h, k=min(k, n - 2), which="SA", tol=tol, v0=_start_vector(n, h.dtype),
                      return_eigenvectors=False)
     return np.sort(vals)
 
@@ -278,7 +289,7 @@ def lowest_eigpairs(h, k: int, tol: float = 1e-14):
         return w[:k], v[:, :k]
     import scipy.sparse.linalg as spl
 
-    w, v = spl.eigsh(h, k=min(k, n - 2), which="SA", tol=tol, v0=np.ones(n, h.dtype) / np.sqrt(n))
+    w, v = spl.eigsh(h, k=min(k, n - 2), which="SA", tol=tol, v0=_start_vector(n, h.dtype))
     o = np.argsort(w)
     return w[o], v[:, o]
 

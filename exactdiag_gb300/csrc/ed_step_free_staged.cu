@@ -13,17 +13,21 @@ int launch_staged(const StepArgs& a, cudaStream_t st) {
     if (a.count <= 0) return ED_OK;
     auto* kern = seg_step_kernel<R, CPLX, 2, MERGED, NR, true>;
     const size_t dyn = (size_t)(kSegThreads / 32) * kSegStageBytes;
-    static int per_sm = -1;  // CTAs per SM with this dynamic shared memory (set once per process)
-    if (per_sm < 0) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return set_error(ED_ERR_INVALID, "seg_step_kernel (staged): device ordinal");
+    // CTAs per SM with this dynamic shared memory, per device (the attribute is set once per device)
+    static int per_sm_of[64] = {};
+    int& per_sm = per_sm_of[dev];
+    if (per_sm < 1) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSegThreads, dyn) != cudaSuccess ||
             per_sm < 1) {
             cudaGetLastError();
+            per_sm = 0;
             return set_error(ED_ERR_CUDA, "seg_step_kernel (staged): shared memory configuration");
         }
     }
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = a.grid < sms * per_sm ? a.grid : sms * per_sm;
     if (grid > a.count) grid = a.count;

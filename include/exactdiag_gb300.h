@@ -69,7 +69,7 @@ int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
  * partial sums are kept per chunk, its recursions then differ in the last bits (a sector still gives
  * the same bits alone and in a batch).  staged_gathers = 1 sends the free-row kernel's gathers through
  * shared memory (cp.async; results unchanged, at most two CTAs per SM).  ED_ERR_INVALID for values out
- * of range. */
+ * of range.  Call it between steps: a new chunk length replaces the sector's step tables. */
 int ed_sector_set_step_shape(ed_sector* s, int rows_per_lane, int chunk_rows, int staged_gathers);
 int ed_sector_get_step_shape(const ed_sector* s, int* rows_per_lane, int* chunk_rows, int* staged_gathers);
 

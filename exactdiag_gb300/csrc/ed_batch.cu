@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(kUpdThreads, 4)
 // straddles two blocks), sector-major in row order; a kind's chunks are kChunkRows long, halved (down
 // to kChunkRows / 8) while the sector's rows of that kind would make fewer chunks than four per SM.
 // H.v chunks: for a free block, its segments class by class (kl = 0 .. P), seg_chunk_rows / kSegWin
-// segments per range (whole rounds of the CTA's warps), each range window by window (kSegWin offsets
-// of every segment); for the other blocks, their row chunks.
+// segments per range (whole rounds of the CTA's warps, two segments per warp), each range window by
+// window (kSegWin offsets of every segment); for the other blocks, their row chunks.
 // Both depend on the sector alone: a sector is cut the same way alone and in a batch, so its
 // per-chunk sums, and with them its recursion, are the same bits either way.  Expanded copies: one
 // per block of Sector::copy_blocks, sector by sector.
@@ -393,8 +393,8 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
             }
             if (kind != kRowsFree) return;
             // segment chunks of a free block: per class, per range of segments (whole rounds of the CTA's
-            // warps), per 64-offset window of a segment -- the windows of one range next to each other,
-            // so that the CTAs working at the same time share the range's records and values
+            // warps, two segments each), per window of kSegWin offsets -- the windows of one range next to
+            // each other, so that the CTAs working at the same time share the range's records and values
             const int Pb = S.view.seg_p;
             const int64_t warps = kSegThreads / 32;
             for (int kl = 0; kl <= Pb; ++kl) {
@@ -403,7 +403,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
                 int64_t nA = 1;  // C(Pb, kl)
                 for (int j = 1; j <= kl; ++j) nA = nA * (Pb - kl + j) / j;
                 const int64_t windows = (nA + kSegWin - 1) / kSegWin;
-                const int64_t per = warps * std::max<int64_t>(1, S.seg_chunk_rows / (warps * kSegWin));
+                const int64_t per = 2 * warps * std::max<int64_t>(1, S.seg_chunk_rows / (2 * warps * kSegWin));
                 for (int64_t g = 0; g < nseg; g += per)
                     for (int64_t pc = 0; pc < windows; ++pc) {
                         BatchChunk c{};

@@ -72,7 +72,7 @@ constexpr int kChunkRows = 8192;
 // chunk of it holds.
 constexpr int kSegThreads = 256;
 constexpr int kSegChunkRows = 16384;
-constexpr int kSegWin = 64;  // offsets of a segment one warp covers in a segment chunk (two rows per lane)
+constexpr int kSegWin = 32;  // offsets of a segment a segment chunk covers (one per lane, in two segments at a time)
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
 enum RowKind : int {

@@ -22,13 +22,16 @@
 //     bits above P) and va per thread; otherwise the full rank of U | V is taken per row.
 //     Stabiliser targets read the expanded copy of the target block (expand_cand_kernel) at the same
 //     rank, with the coset's first phase folded in.
-// A warp takes one 32-row piece of a segment (lane = offset in the segment), or several whole
-// segments of at most 16 rows, and walks the chunk's segments with the CTA's other warps; warps never
-// wait on one another inside a chunk, and every per-segment loop bound is the same for all lanes of a
-// warp.  The per-lane terms of a chunk live in shared memory (every warp maps its lanes to the same
-// offsets).  While a warp works on one segment, the next segment's record is copied into shared
-// memory (cp.async) and its row value loaded, so a row's gathers wait on one round trip per group
-// (low bonds, high bonds four at a time, cross bonds, hops) rather than on chains of dependent loads.
+// A chunk covers a 32-offset window of a range of segments (lane = offset in the window); a warp takes
+// two segments at a time (a lane's two rows share the offset, so the per-offset terms are read once
+// for both) and walks the range with the CTA's other warps; warps never wait on one another inside a
+// chunk, and every per-segment loop bound is the same for all lanes of a warp.  32-offset windows
+// keep the lanes busy on the classes whose C(P, kl) is not a multiple of 64 (210 rows: 94 % against
+// 82 % with 64-offset windows) and the low lists, padded to the window's longest, shorter.  The
+// per-lane terms of a chunk live in shared memory (every warp maps its lanes to the same offsets).
+// While a warp works on one pair, the next pair's records are copied into shared memory (cp.async)
+// and its row values loaded, so a row's gathers wait on one round trip per group (low bonds, high
+// bonds four at a time, cross bonds, hops) rather than on chains of dependent loads.
 // The key table is not read: a free row's configuration follows from its index.
 //
 // Per-row sums of the step (ed_step.cuh) are kept per thread in plain FP32 (FP64) over four rows and
@@ -229,12 +232,14 @@ __device__ __forceinline__ R seg_slot_ci(const SegSlot<R, CPLX>& S) {
     else return R(0);
 }
 
-// The fused step over segment chunks: a chunk is (free block, class kl, 64-offset window, range of
-// segments); warp w of the CTA takes segments begin + w, begin + w + 8, ... and, in each, the rows at
-// offsets t = window + lane and t + 32.  NR rows are worked on together (their gathers in flight
-// at once, the segment's record words read once for both); NR = 1 takes the two rows one after
-// the other.  MERGED: rung and leg exchanges share one coefficient (J_rung = J_leg), so each row keeps
-// one exchange sum over one list per bond class; otherwise every element picks its coefficient.
+// The fused step over segment chunks: a chunk is (free block, class kl, 32-offset window, range of
+// segments); warp w of the CTA takes the segment pairs (begin + 2w, begin + 2w + 1), then 16 segments
+// further, ... and, in both segments of a pair, the row at offset t = window + lane.  The per-offset
+// tables (low-bond partners, cross and hop parts) are read once for the two rows; each row reads its
+// own segment's record.  NR = 2 works on the two rows together (their gathers in flight at once);
+// NR = 1 takes them one after the other.  MERGED: rung and leg exchanges share one coefficient
+// (J_rung = J_leg), so each row keeps one exchange sum over one list per bond class; otherwise every
+// element picks its coefficient.
 template <typename R, bool CPLX, int MINB, bool MERGED, int NR, bool STAGED = false>
 __global__ void __launch_bounds__(kSegThreads, MINB)
     seg_step_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
@@ -254,16 +259,17 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     // hop slots of the chunk: the kind-0 hops then dummies up to a multiple of four, the same for kind 1
     // (nb 1 or 2); a dummy reads the block's first element with coefficient 0
     __shared__ __align__(16) SegSlot<R, CPLX> s_slot[kSegHopSlots];
-    // per-offset terms of the chunk's window (column j = offset - window; every warp maps its lanes to
-    // the same columns): a column past the class's rows repeats column j - 32, so its reads stay valid
+    // per-offset terms of the chunk's window (column = lane = offset - window): a column past the
+    // class's rows repeats column 0, so its reads stay valid
     __shared__ uint8_t s_al[kSegLowMax][kSegWin];      // partners of the antiparallel bonds below P (rung
                                                        // first), padded with the offset itself
     __shared__ uint8_t s_xo[kSegMaxX][kSegWin];        // cross bond c: rank_P(Lo ^ low end) (0 past nX)
     __shared__ uint16_t s_hc[kSegHopSlots][kSegWin];   // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA
     __shared__ uint32_t s_lane[kSegWin];               // Lo | lob << 16 (cross-bond low-end spins)
     __shared__ uint32_t s_cnt[kSegWin];                // nr | nlow << 8 (antiparallel bonds below P)
-    __shared__ int s_maxw[2];                          // longest low list of each half, in fours
-    __shared__ __align__(16) uint32_t s_rec[kWarps][2][kSegRecMax];  // per warp: this and the next record
+    __shared__ int s_maxw;                             // longest low list of the window, in fours
+    // per warp: this pair's and the next pair's records
+    __shared__ __align__(16) uint32_t s_rec[kWarps][2][2][kSegRecMax];
     const int P = views[0].seg_p;
     const uint32_t amask = (1u << P) - 1u;
     const uint32_t* __restrict__ comb = views[0].comb;
@@ -296,7 +302,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
         const int nA = (int)comb[kl * kCombStride + P];
         const int win = kSegWin * ch.piece;
-        const int nact = min(32, nA - win);  // lanes with a first row
+        const int nact = min(32, nA - win);  // lanes with rows
         __syncthreads();  // the previous chunk's rows are done with the shared tables
         {
             const uint4* src = reinterpret_cast<const uint4*>(Sp->seg + ch.block);
@@ -308,7 +314,11 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int64_t bstart = s_desc.start;
         T* const x = reinterpret_cast<T*>(v) + offs[ch.sec];
         const T* const xb = x + bstart;
+        const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
         {  // the chunk's tables: hop records, per-offset terms, hop slots
+            // the offset whose terms column `lane` holds: its own, or (past the class's rows) the window's first
+            const int tsrc = win + lane < nA ? win + lane : win;
+            const uint32_t lo_c = s_ut[s_utoff[kl] + tsrc];
             if (warp == 2 && lane < kMaxHops) {
                 // every hop gets a record: absent hops (and those past nhop) read a valid element with
                 // coefficient 0
@@ -351,13 +361,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                         F.cr = G.e == 0 ? cf : -cf;
                     }
                 }
-            }
-            // the offset whose terms column j holds: its own, or (past the class's rows) column j - 32's
-            const int jcol = 32 * warp + lane;  // warps 0 and 1
-            int tsrc = win + jcol;
-            if (warp < 2 && tsrc >= nA) tsrc = (win + lane < nA) ? win + lane : win;
-            const uint32_t lo_c = (warp < 2 && tsrc < nA) ? s_ut[s_utoff[kl] + tsrc] : 0u;
-            if (warp < 2) {
+            } else if (warp == 0) {
                 // bonds below P: the antiparallel ones' partners, rung bonds first, padded with the offset
                 // itself up to the table's length (read in fours, the padding taken back out after the sums)
                 int nr = 0, nlow = 0;
@@ -365,26 +369,28 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 for (int i = 0; i < nAb; ++i) {
                     const uint32_t f = s_desc.fA[i], sb = lo_c & f;
                     if (sb != 0u && sb != f) {
-                        s_al[nlow++][jcol] = s_rt[lo_c ^ f];
+                        s_al[nlow++][lane] = s_rt[lo_c ^ f];
                         if (i < nAr) ++nr;
                     }
                 }
-                for (int q = nlow; q < kSegLowMax; ++q) s_al[q][jcol] = (uint8_t)tsrc;
+                for (int q = nlow; q < kSegLowMax; ++q) s_al[q][lane] = (uint8_t)tsrc;
                 const int mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow);
+                s_cnt[lane] = (uint32_t)nr | ((uint32_t)nlow << 8);
+                if (lane == 0) s_maxw = (mx + 3) & ~3;
+            } else if (warp == 1) {
+                // bonds across P: the partner's low part and this offset's spin at the low end
                 uint32_t lob = 0;
                 for (int cc = 0; cc < kSegMaxX; ++cc) {
                     const uint32_t a = s_desc.cX[cc][0];
                     if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
-                    s_xo[cc][jcol] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
+                    s_xo[cc][lane] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
                 }
-                s_lane[jcol] = lo_c | (lob << 16);
-                s_cnt[jcol] = (uint32_t)nr | ((uint32_t)nlow << 8);
-                if (lane == 0) s_maxw[warp] = (mx + 3) & ~3;
+                s_lane[lane] = lo_c | (lob << 16);
             }
             __syncthreads();
-            const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
-            if (warp < 2) {
-                for (int sl = 0; sl < n04 + n124; ++sl) {
+            if (warp != 2) {
+                // hop slots, spread over the other warps
+                for (int sl = warp < 2 ? warp : warp - 1; sl < n04 + n124; sl += kWarps - 1) {
                     const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
                     uint32_t hc = 0;
                     if (h >= 0 && s_hop[h].kind != 3) {
@@ -392,9 +398,9 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                         const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
                         hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
                     }
-                    s_hc[sl][jcol] = (uint16_t)hc;
+                    s_hc[sl][lane] = (uint16_t)hc;
                 }
-            } else if (warp == 2 && lane < n04 + n124) {
+            } else if (lane < n04 + n124) {
                 const int sl = lane;
                 const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
                 SegSlot<R, CPLX>& S = s_slot[sl];
@@ -405,9 +411,8 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             }
             __syncthreads();
         }
-        const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
 
-        const int smax = max(s_maxw[0], s_maxw[1]);  // low lists read, in fours
+        const int smax = s_maxw;  // low lists read, in fours
         const uint32_t rec_len = s_desc.rec_len, xo = s_desc.xo;
         const uint32_t* __restrict__ rec0 = Sp->seg_rec + s_desc.rec + (int64_t)Sp->seg_off[kl] * rec_len;
         const uint32_t* __restrict__ segb = Sp->seg_base + Sp->seg_off[kl];
@@ -416,210 +421,224 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         T* const y = reinterpret_cast<T*>(other) + offs[ch.sec] + bstart;
         const T* const yp = first ? nullptr : reinterpret_cast<const T*>(vprev) + offs[ch.sec] + bstart;
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
-        // per half h of the window: this lane's offset, whether it is a row, the offset read for it
-        int tt[2];
-        bool act[2];
-        uint32_t lnw[2], cnt[2];  // s_lane and s_cnt of the two columns (fields unpacked where used)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int t = win + lane + 32 * h;
-            act[h] = t < nA;
-            tt[h] = act[h] ? t : win + lane;
-            lnw[h] = s_lane[lane + 32 * h];
-            cnt[h] = s_cnt[lane + 32 * h];
-        }
-        uint32_t* const srec0 = s_rec[warp][0];
-        uint32_t* const srec1 = s_rec[warp][1];
+        // this lane's offset (rows in both segments of a pair) and its column of the tables
+        const int t = win + lane;
+        const uint32_t lnw = s_lane[lane], cnt = s_cnt[lane];
+        const int nlow = (int)(cnt >> 8), nrl = (int)(cnt & 255u);
+        const T* const xt = xb + t;
 
         Accum<R> acc[kReduceSlots];
         R pend[kReduceSlots] = {R(0), R(0), R(0), R(0)};
         int npend = 0;
 
-        // the next segment's record is copied into shared memory, and its rows' values and v_{k-1}
-        // loaded, while this one is worked on; the active lanes together copy every word of a record
-        // segment indices of a class fit 32 bits (SectorView::seg_off)
+        // the next pair's records are copied into shared memory, and its rows' values and v_{k-1}
+        // loaded, while this pair is worked on; the active lanes together copy every word of a record
+        // (segment indices of a class fit 32 bits: SectorView::seg_off)
         const int gend = (int)ch.end;
-        int g = lane < nact ? (int)ch.begin + warp : gend;  // lanes without a row skip to the reduction
-        if (g < gend)
-            for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
-                seg_cp_async16(srec0 + w4, rec0 + (uint32_t)g * rec_len + w4);
-        seg_cp_commit();
-        uint32_t base = 0;
+        int g = lane < nact ? (int)ch.begin + 2 * warp : gend;  // lanes without rows skip to the reduction
+        auto copy_pair = [&](int gg, uint32_t* dst) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+                if (gg + r < gend)
+                    for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
+                        seg_cp_async16(dst + r * kSegRecMax + w4, rec0 + (uint32_t)(gg + r) * rec_len + w4);
+        };
+        uint32_t base[2] = {0u, 0u};
         R xr[2] = {R(0), R(0)}, xi[2] = {R(0), R(0)}, pr[2] = {R(0), R(0)}, pi[2] = {R(0), R(0)};
         if (g < gend) {
-            base = __ldg(segb + g);
+            copy_pair(g, s_rec[warp][0][0]);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                seg_ld<R, CPLX>(xb + base + tt[h], xr[h], xi[h]);
-                if (!first) seg_ld<R, CPLX>(yp + base + tt[h], pr[h], pi[h]);
+            for (int r = 0; r < 2; ++r) {
+                base[r] = __ldg(segb + (g + r < gend ? g + r : g));
+                seg_ld<R, CPLX>(xt + base[r], xr[r], xi[r]);
+                if (!first) seg_ld<R, CPLX>(yp + base[r] + t, pr[r], pi[r]);
             }
         }
-        for (int it = 0; g < gend; ++it, g += kWarps) {
-            const uint32_t* const sw = (it & 1) ? srec1 : srec0;
-            const int gn = g + kWarps;
-            if (gn < gend) {
-                uint32_t* const dst = (it & 1) ? srec0 : srec1;
-                for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
-                    seg_cp_async16(dst + w4, rec0 + (uint32_t)gn * rec_len + w4);
-            }
+        seg_cp_commit();
+        for (int it = 0; g < gend; ++it, g += 2 * kWarps) {
+            const bool act1 = g + 1 < gend;  // the pair's second segment exists (warp-uniform)
+            const uint32_t* const sw[2] = {s_rec[warp][it & 1][0], s_rec[warp][it & 1][act1 ? 1 : 0]};
+            const int gn = g + 2 * kWarps;
+            if (gn < gend) copy_pair(gn, s_rec[warp][(it + 1) & 1][0]);
             seg_cp_commit();
-            uint32_t nbase = 0;
+            uint32_t nbase[2] = {0u, 0u};
             R nxr[2] = {R(0), R(0)}, nxi[2] = {R(0), R(0)}, npr[2] = {R(0), R(0)}, npi[2] = {R(0), R(0)};
             if (gn < gend) {
-                nbase = __ldg(segb + gn);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    seg_ld<R, CPLX>(xb + nbase + tt[h], nxr[h], nxi[h]);
-                    if (!first) seg_ld<R, CPLX>(yp + nbase + tt[h], npr[h], npi[h]);
+                for (int r = 0; r < 2; ++r) {
+                    nbase[r] = __ldg(segb + (gn + r < gend ? gn + r : gn));
+                    seg_ld<R, CPLX>(xt + nbase[r], nxr[r], nxi[r]);
+                    if (!first) seg_ld<R, CPLX>(yp + nbase[r] + t, npr[r], npi[r]);
                 }
             }
-            seg_cp_wait<1>();  // this segment's record has arrived (the next one may be in flight)
+            seg_cp_wait<1>();  // this pair's records have arrived (the next pair's may be in flight)
             __syncwarp(__activemask());
 
-            const uint32_t w1 = sw[1];
-            const int zb = (int)(w1 & 255u), zbr = (int)((w1 >> 8) & 255u);
-            const int zb4 = (zb + 3) & ~3;
-            const uint32_t hib = w1 >> 16;
-            const T* const xs = xb + base;  // the segment
+            int zb[2], zbr[2], zb4[2];
+            uint32_t xm[2];
 #pragma unroll
-            for (int h0 = 0; h0 < 2; h0 += NR) {
-                // ---- rows t = window + lane + 32 (h0 + r): y = H x - beta v_{k-1}
-                const T* xt[NR];
-                uint32_t xm[NR];
+            for (int r = 0; r < 2; ++r) {
+                const uint32_t w1 = sw[r][1];
+                zb[r] = (int)(w1 & 255u);
+                zbr[r] = (int)((w1 >> 8) & 255u);
+                zb4[r] = (zb[r] + 3) & ~3;
+                xm[r] = ((lnw >> 16) ^ (w1 >> 16)) & xall;  // cross bonds antiparallel in row r
+            }
+#pragma unroll
+            for (int r0 = 0; r0 < 2; r0 += NR) {
+                if (NR == 1 && r0 == 1 && !act1) break;
+                // ---- the rows at offset t of segments g + r0 (+ 1): y = H x - beta v_{k-1}
+                const T* xs[NR];
                 R er[NR], ei[NR], lr[NR], li[NR], hr[NR], hi[NR];
 #pragma unroll
                 for (int r = 0; r < NR; ++r) {
-                    xt[r] = xb + tt[h0 + r];
-                    xm[r] = ((lnw[h0 + r] >> 16) ^ hib) & xall;
+                    xs[r] = xb + base[r0 + r];
                     er[r] = ei[r] = lr[r] = li[r] = hr[r] = hi[r] = R(0);
                 }
                 if constexpr (!STAGED) {
-                    // exchange bonds below P: partners in the same segment, four loads at a time per row
+                    // exchange bonds below P: partners in the row's own segment, one table read for the rows
                     for (int q0 = 0; q0 < smax; q0 += 4) {
                         R vr[NR][4], vi[NR][4];
-    #pragma unroll
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint32_t o = s_al[q0 + u][lane];
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xs[r] + o, vr[r][u], vi[r][u]);
+                        }
+#pragma unroll
                         for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r)
-                                seg_ld<R, CPLX>(xs + (uint32_t)s_al[q0 + u][lane + 32 * (h0 + r)], vr[r][u], vi[r][u]);
-    #pragma unroll
-                        for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < (int)(cnt[h0 + r] & 255u), vr[r][u], vi[r][u]);
+#pragma unroll
+                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < nrl, vr[r][u], vi[r][u]);
                     }
-                    // exchange bonds at or above P: the partner segments at the same offsets, four at a time
-                    for (int q0 = 0; q0 < zb4; q0 += 4) {
+                    // exchange bonds at or above P: the partner segments at the same offset, four at a
+                    // time; the rows together up to the shorter list, then each row's rest
+                    auto high4 = [&](int r, int q0, R (&vr)[4], R (&vi)[4]) {
+                        const uint4 pw = *reinterpret_cast<const uint4*>(sw[r0 + r] + 4 + q0);  // 16-byte aligned
+                        seg_ld<R, CPLX>(xt + pw.x, vr[0], vi[0]);
+                        seg_ld<R, CPLX>(xt + pw.y, vr[1], vi[1]);
+                        seg_ld<R, CPLX>(xt + pw.z, vr[2], vi[2]);
+                        seg_ld<R, CPLX>(xt + pw.w, vr[3], vi[3]);
+                    };
+                    const int zc = NR == 2 ? min(zb4[r0], zb4[r0 + NR - 1]) : zb4[r0];
+                    for (int q0 = 0; q0 < zc; q0 += 4) {
                         R vr[NR][4], vi[NR][4];
-                        const uint4 pw = *reinterpret_cast<const uint4*>(sw + 4 + q0);  // 16-byte aligned
-                        const uint32_t pq[4] = {pw.x, pw.y, pw.z, pw.w};
-    #pragma unroll
+#pragma unroll
+                        for (int r = 0; r < NR; ++r) high4(r, q0, vr[r], vi[r]);
+#pragma unroll
                         for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xt[r] + pq[u], vr[r][u], vi[r][u]);
-    #pragma unroll
-                        for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr, vr[r][u], vi[r][u]);
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr[r0 + r], vr[r][u], vi[r][u]);
                     }
+#pragma unroll
+                    for (int r = 0; r < NR; ++r)
+                        for (int q0 = zc; q0 < zb4[r0 + r]; q0 += 4) {
+                            R vr[4], vi[4];
+                            high4(r, q0, vr, vi);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < zbr[r0 + r], vr[u], vi[u]);
+                        }
                     // bonds across P, antiparallel when the two ends' spins differ (otherwise the row itself is read)
                     for (int c0 = 0; c0 < nX4; c0 += 4) {
                         R vr[NR][4], vi[NR][4];
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             const int cc = c0 + u;
-                            const uint32_t pw = sw[xo + cc];
-    #pragma unroll
+                            const uint32_t xoc = s_xo[cc][lane];
+#pragma unroll
                             for (int r = 0; r < NR; ++r) {
-                                const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
-                                const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
-                                                   (~on & (base + (uint32_t)tt[h0 + r]));
+                                const uint32_t pw = sw[r0 + r][xo + cc];
+                                const uint32_t on = 0u - ((xm[r0 + r] >> cc) & 1u);  // all ones when antiparallel
+                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)t));
                                 seg_ld<R, CPLX>(xb + o, vr[r][u], vi[r][u]);
                             }
                         }
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u)
-    #pragma unroll
+#pragma unroll
                             for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], c0 + u < nXr, vr[r][u], vi[r][u]);
                     }
                     // hops, four at a time: kind 0 (r = sb + rank_P(V)), then kind 1 (r = sb[vbi] + rank_P(ua | va))
                     for (int h4 = 0; h4 < n04; h4 += 4) {
                         R vr[NR][4], vi[NR][4];
                         SegSlot<R, CPLX> S[4];
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             S[u] = s_slot[h4 + u];
-                            const uint32_t sb = sw[S[u].off];
-    #pragma unroll
+                            const uint32_t hc = s_hc[h4 + u][lane];
+#pragma unroll
                             for (int r = 0; r < NR; ++r)
-                                seg_ld<R, CPLX>(S[u].tp + (sb + s_hc[h4 + u][lane + 32 * (h0 + r)]), vr[r][u], vi[r][u]);
+                                seg_ld<R, CPLX>(S[u].tp + (sw[r0 + r][S[u].off] + hc), vr[r][u], vi[r][u]);
                         }
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r) {
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
                                 seg_hop_acc<R, CPLX>(hr[r], hi[r], S[u].cr, seg_slot_ci(S[u]), vr[r][u], vi[r][u]);
-                            }
                     }
                     for (int h4 = n04; h4 < n04 + n124; h4 += 4) {
                         R vr[NR][4], vi[NR][4];
                         SegSlot<R, CPLX> S[4];
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             S[u] = s_slot[h4 + u];
-                            const uint32_t ua = sw[S[u].off];
-    #pragma unroll
+                            const uint32_t hc = s_hc[h4 + u][lane];
+                            const uint32_t wv = S[u].off + 1u + (hc >> kSegA), va = hc & (kSegLow - 1u);
+#pragma unroll
                             for (int r = 0; r < NR; ++r) {
-                                const uint32_t hc = s_hc[h4 + u][lane + 32 * (h0 + r)];
-                                const uint32_t rr = sw[S[u].off + 1u + (hc >> kSegA)] + s_rt[ua | (hc & (kSegLow - 1u))];
+                                const uint32_t rr = sw[r0 + r][wv] + s_rt[sw[r0 + r][S[u].off] | va];
                                 seg_ld<R, CPLX>(S[u].tp + rr, vr[r][u], vi[r][u]);
                             }
                         }
-    #pragma unroll
+#pragma unroll
                         for (int u = 0; u < 4; ++u)
-    #pragma unroll
-                            for (int r = 0; r < NR; ++r) {
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
                                 seg_hop_acc<R, CPLX>(hr[r], hi[r], S[u].cr, seg_slot_ci(S[u]), vr[r][u], vi[r][u]);
-                            }
                     }
                 } else {
                     // every gather of the rows goes to shared memory by cp.async, up to kScap slots per
                     // pass: all in flight together, one wait, then the sums read them back.  Slots:
-                    // low bonds [0, e0), high [e0, e1), cross [e1, e2), hop slots [e2, e3)
+                    // low bonds [0, e0), high [e0, e1) (the pair's longer list: the shorter row skips
+                    // the slots past its own, so each row adds the terms of the unstaged kernel in its
+                    // order), cross [e1, e2), hop slots [e2, e3)
                     T* const stg = reinterpret_cast<T*>(seg_stage_smem) + (size_t)warp * kScap * kCols;
-                    const int e0 = smax, e1 = e0 + zb4, e2 = e1 + nX4, e3 = e2 + n04 + n124;
+                    const int zs = NR == 2 ? max(zb4[r0], zb4[r0 + NR - 1]) : zb4[r0];
+                    const int e0 = smax, e1 = e0 + zs, e2 = e1 + nX4, e3 = e2 + n04 + n124;
                     for (int p0 = 0; p0 < e3; p0 += kScap) {
                         const int p1 = min(e3, p0 + kScap);
-                        for (int sl = p0; sl < min(p1, e0); ++sl)
+                        for (int sl = p0; sl < min(p1, e0); ++sl) {
+                            const uint32_t o = s_al[sl][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r)
-                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r,
-                                                     xs + (uint32_t)s_al[sl][lane + 32 * (h0 + r)]);
-                        for (int sl = max(p0, e0); sl < min(p1, e1); ++sl) {
-                            const uint32_t pw = sw[4 + sl - e0];
-#pragma unroll
-                            for (int r = 0; r < NR; ++r)
-                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xt[r] + pw);
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xs[r] + o);
                         }
+                        for (int sl = max(p0, e0); sl < min(p1, e1); ++sl)
+#pragma unroll
+                            for (int r = 0; r < NR; ++r)
+                                if (sl - e0 < zb4[r0 + r])
+                                    seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xt + sw[r0 + r][4 + sl - e0]);
                         for (int sl = max(p0, e1); sl < min(p1, e2); ++sl) {
                             const int cc = sl - e1;
-                            const uint32_t pw = sw[xo + cc];
+                            const uint32_t xoc = s_xo[cc][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
-                                const uint32_t on = 0u - ((xm[r] >> cc) & 1u);  // all ones when antiparallel
-                                const uint32_t o = (on & (pw + s_xo[cc][lane + 32 * (h0 + r)])) |
-                                                   (~on & (base + (uint32_t)tt[h0 + r]));
+                                const uint32_t pw = sw[r0 + r][xo + cc];
+                                const uint32_t on = 0u - ((xm[r0 + r] >> cc) & 1u);  // all ones when antiparallel
+                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)t));
                                 seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xb + o);
                             }
                         }
                         for (int sl = max(p0, e2); sl < p1; ++sl) {
                             const int hs = sl - e2;  // hop slot: kind 0 below n04, kind 1 from n04
                             const SegSlot<R, CPLX>& S = s_slot[hs];
-                            const uint32_t w0 = sw[S.off];
+                            const uint32_t hc = s_hc[hs][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
-                                const uint32_t hc = s_hc[hs][lane + 32 * (h0 + r)];
+                                const uint32_t w0 = sw[r0 + r][S.off];
                                 const uint32_t rr = hs < n04 ? w0 + hc
-                                                             : sw[S.off + 1u + (hc >> kSegA)] +
+                                                             : sw[r0 + r][S.off + 1u + (hc >> kSegA)] +
                                                                    s_rt[w0 | (hc & (kSegLow - 1u))];
                                 seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, S.tp + rr);
                             }
@@ -630,10 +649,11 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                         for (int sl = p0; sl < min(p1, e2); ++sl)
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
+                                if (sl >= e0 && sl < e1 && sl - e0 >= zb4[r0 + r]) continue;  // past the row's high list
                                 R vr, vi;
                                 seg_ld_shared<R, CPLX>(stg + (sl - p0) * kCols + lane + 32 * r, vr, vi);
-                                const bool rung = sl < e0 ? sl < (int)(cnt[h0 + r] & 255u)
-                                                          : (sl < e1 ? sl - e0 < zbr : sl - e1 < nXr);
+                                const bool rung = sl < e0 ? sl < nrl
+                                                          : (sl < e1 ? sl - e0 < zbr[r0 + r] : sl - e1 < nXr);
                                 seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], rung, vr, vi);
                             }
                         for (int sl = max(p0, e2); sl < p1; ++sl) {
@@ -654,11 +674,11 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll 1
                     for (int hh = n0 + n12; hh < nhop; ++hh) {
                         const SegHop<R, CPLX>& F = s_hop[hh];
+                        const uint32_t V =
+                            seg_perm(lnw & 0xffffu, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
 #pragma unroll
                         for (int r = 0; r < NR; ++r) {
-                            const uint32_t V =
-                                seg_perm(lnw[h0 + r] & 0xffffu, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                            const uint32_t rr = spin_rank(sw[s_desc.hop_off[hh]] | V, RT, Nd);
+                            const uint32_t rr = spin_rank(sw[r0 + r][s_desc.hop_off[hh]] | V, RT, Nd);
                             R vr, vi;
                             seg_ld<R, CPLX>(F.tp + rr, vr, vi);
                             seg_hop_acc<R, CPLX>(hr[r], hi[r], F.cr, F.ci, vr, vi);
@@ -667,42 +687,41 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
 #pragma unroll
                 for (int r = 0; r < NR; ++r) {
-                    const int hh = h0 + r;
-                    const int nlow = (int)(cnt[hh] >> 8), nr = (int)(cnt[hh] & 255u);
+                    const int rr = r0 + r;
                     // the padding read the row itself (in split mode into the leg sum; a parallel cross
                     // bond into its own kind's sum): take it back out; then the diagonal, -J/2 per
                     // antiparallel bond
-                    const int pads = (smax - nlow) + (zb4 - zb) + __popc(~xm[r] & x4mask & ~(MERGED ? 0u : xrmask));
+                    const int pads = (smax - nlow) + (zb4[rr] - zb[rr]) + __popc(~xm[rr] & x4mask & ~(MERGED ? 0u : xrmask));
                     R h_r, h_i;
                     if constexpr (MERGED) {
-                        const R e_r = er[r] - (R)pads * xr[hh];
-                        const R e_i = CPLX ? ei[r] - (R)pads * xi[hh] : R(0);
-                        const R diag = -wr * (R)(nlow + zb + __popc(xm[r]));
-                        h_r = wr * e_r + hr[r] + diag * xr[hh];
-                        h_i = CPLX ? wr * e_i + hi[r] + diag * xi[hh] : R(0);
+                        const R e_r = er[r] - (R)pads * xr[rr];
+                        const R e_i = CPLX ? ei[r] - (R)pads * xi[rr] : R(0);
+                        const R diag = -wr * (R)(nlow + zb[rr] + __popc(xm[rr]));
+                        h_r = wr * e_r + hr[r] + diag * xr[rr];
+                        h_i = CPLX ? wr * e_i + hi[r] + diag * xi[rr] : R(0);
                     } else {
-                        const R rpad = (R)__popc(~xm[r] & xrmask);
-                        const R a_r = er[r] - rpad * xr[hh], a_i = CPLX ? ei[r] - rpad * xi[hh] : R(0);
-                        const R l_r = lr[r] - (R)pads * xr[hh], l_i = CPLX ? li[r] - (R)pads * xi[hh] : R(0);
-                        const int anr = nr + zbr + __popc(xm[r] & xrmask);
-                        const int anl = (nlow - nr) + (zb - zbr) + __popc(xm[r] & ~xrmask);
+                        const R rpad = (R)__popc(~xm[rr] & xrmask);
+                        const R a_r = er[r] - rpad * xr[rr], a_i = CPLX ? ei[r] - rpad * xi[rr] : R(0);
+                        const R l_r = lr[r] - (R)pads * xr[rr], l_i = CPLX ? li[r] - (R)pads * xi[rr] : R(0);
+                        const int anr = nrl + zbr[rr] + __popc(xm[rr] & xrmask);
+                        const int anl = (nlow - nrl) + (zb[rr] - zbr[rr]) + __popc(xm[rr] & ~xrmask);
                         const R diag = -(wr * (R)anr + wl * (R)anl);
-                        h_r = wr * a_r + wl * l_r + hr[r] + diag * xr[hh];
-                        h_i = CPLX ? wr * a_i + wl * l_i + hi[r] + diag * xi[hh] : R(0);
+                        h_r = wr * a_r + wl * l_r + hr[r] + diag * xr[rr];
+                        h_i = CPLX ? wr * a_i + wl * l_i + hi[r] + diag * xi[rr] : R(0);
                     }
-                    if (act[hh]) {
-                        const R y_r = h_r - beta * pr[hh];
-                        const R y_i = CPLX ? h_i - beta * pi[hh] : R(0);
-                        st<R, CPLX>(y, (int64_t)base + tt[hh], y_r, y_i);
-                        pend[0] = fma_r(xr[hh], h_r, pend[0]);
+                    if (rr == 0 || act1) {
+                        const R y_r = h_r - beta * pr[rr];
+                        const R y_i = CPLX ? h_i - beta * pi[rr] : R(0);
+                        st<R, CPLX>(y, (int64_t)base[rr] + t, y_r, y_i);
+                        pend[0] = fma_r(xr[rr], h_r, pend[0]);
                         pend[1] = fma_r(y_r, y_r, pend[1]);
-                        pend[2] = fma_r(xr[hh], y_r, pend[2]);
-                        pend[3] = fma_r(xr[hh], xr[hh], pend[3]);
+                        pend[2] = fma_r(xr[rr], y_r, pend[2]);
+                        pend[3] = fma_r(xr[rr], xr[rr], pend[3]);
                         if constexpr (CPLX) {
-                            pend[0] = fma_r(xi[hh], h_i, pend[0]);
+                            pend[0] = fma_r(xi[rr], h_i, pend[0]);
                             pend[1] = fma_r(y_i, y_i, pend[1]);
-                            pend[2] = fma_r(xi[hh], y_i, pend[2]);
-                            pend[3] = fma_r(xi[hh], xi[hh], pend[3]);
+                            pend[2] = fma_r(xi[rr], y_i, pend[2]);
+                            pend[3] = fma_r(xi[rr], xi[rr], pend[3]);
                         }
                     }
                 }
@@ -716,14 +735,14 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 }
                 npend = 0;
             }
-            __syncwarp(__activemask());  // every lane is done with this buffer before it is refilled
-            base = nbase;
+            __syncwarp(__activemask());  // every lane is done with this pair's buffer before it is refilled
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                xr[h] = nxr[h];
-                xi[h] = nxi[h];
-                pr[h] = npr[h];
-                pi[h] = npi[h];
+            for (int r = 0; r < 2; ++r) {
+                base[r] = nbase[r];
+                xr[r] = nxr[r];
+                xi[r] = nxi[r];
+                pr[r] = npr[r];
+                pi[r] = npi[r];
             }
         }
         seg_cp_wait<0>();

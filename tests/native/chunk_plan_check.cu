@@ -1,6 +1,6 @@
 // Host check of the step layout (ed_batch.cu: plan_chunks) on synthetic sectors: row chunks tile
 // every sector's rows, never straddle two blocks and follow the per-kind length rule (pinned on two
-// hand-built sectors as well); segment chunks tile every class and 64-offset window of every free block
+// hand-built sectors as well); segment chunks tile every class and offset window of every free block
 // in whole rounds of the CTA's warps; a sector is cut the same way alone and inside a batch (what keeps batched
 // and sequential recursions bit-identical); every listed block gets one expanded copy, and
 // stabiliser chunks point at their block's copy.  Built with nvcc (the file's kernels are compiled
@@ -182,7 +182,7 @@ int main() {
                 const int64_t nseg = (int64_t)secs[s].host_seg_off[a.kl + 1] - secs[s].host_seg_off[a.kl];
                 const int64_t nA = binom(P, a.kl);
                 const int64_t pieces = (nA + kSegWin - 1) / kSegWin;
-                const int64_t round = kSegThreads / 32;
+                const int64_t round = 2 * (kSegThreads / 32);  // two segments per warp
                 expect(a.piece >= 0 && a.piece < pieces, "window inside the segment", trial, c);
                 int64_t& next = seg_next[a.block][a.kl * 8 + a.piece];
                 expect(a.begin == next && a.end > a.begin && a.end <= nseg, "segment chunks tile their class", trial, c);

@@ -160,6 +160,29 @@ __device__ __forceinline__ void seg_ld_shared(const typename Vec<R, CPLX>::T* p,
 }
 
 
+// A thread's running sum kept in shared memory: two words for FP32 ([0] high, [1] low part), one for FP64.
+constexpr int seg_acc_words(int real_size) { return real_size == 4 ? 2 : 1; }
+template <typename R>
+__device__ __forceinline__ Accum<R> seg_acc_load(const R (&s)[seg_acc_words(sizeof(R))][kSegThreads], int i) {
+    Accum<R> a;
+    if constexpr (sizeof(R) == 4) {
+        a.hi = s[0][i];
+        a.lo = s[1][i];
+    } else {
+        a.s = s[0][i];
+    }
+    return a;
+}
+template <typename R>
+__device__ __forceinline__ void seg_acc_store(R (&s)[seg_acc_words(sizeof(R))][kSegThreads], int i, const Accum<R>& a) {
+    if constexpr (sizeof(R) == 4) {
+        s[0][i] = a.hi;
+        s[1][i] = a.lo;
+    } else {
+        s[0][i] = a.s;
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ void fold(Accum<R>& a, R p);
 template <>
@@ -270,6 +293,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     __shared__ int s_maxw;                             // longest low list of the window, in fours
     // per warp: this pair's and the next pair's records
     __shared__ __align__(16) uint32_t s_rec[kWarps][2][2][kSegRecMax];
+    __shared__ R s_acc[kReduceSlots][seg_acc_words(sizeof(R))][kSegThreads];  // per thread: the step's sums
     const int P = views[0].seg_p;
     const uint32_t amask = (1u << P) - 1u;
     const uint32_t* __restrict__ comb = views[0].comb;
@@ -427,9 +451,12 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int nlow = (int)(cnt >> 8), nrl = (int)(cnt & 255u);
         const T* const xt = xb + t;
 
-        Accum<R> acc[kReduceSlots];
+        // the step's running sums (float-float for FP32) wait in shared memory between folds: eight
+        // registers fewer in the row loop, which lets the 4-CTA variant run without spills
         R pend[kReduceSlots] = {R(0), R(0), R(0), R(0)};
         int npend = 0;
+#pragma unroll
+        for (int q = 0; q < kReduceSlots; ++q) seg_acc_store<R>(s_acc[q], threadIdx.x, Accum<R>{});
 
         // the next pair's records are copied into shared memory, and its rows' values and v_{k-1}
         // loaded, while this pair is worked on; the active lanes together copy every word of a record
@@ -730,7 +757,9 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             if (npend >= 4) {
 #pragma unroll
                 for (int q = 0; q < kReduceSlots; ++q) {
-                    fold<R>(acc[q], pend[q]);
+                    Accum<R> a = seg_acc_load<R>(s_acc[q], threadIdx.x);
+                    fold<R>(a, pend[q]);
+                    seg_acc_store<R>(s_acc[q], threadIdx.x, a);
                     pend[q] = R(0);
                 }
                 npend = 0;
@@ -746,8 +775,12 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             }
         }
         seg_cp_wait<0>();
+        Accum<R> acc[kReduceSlots];
 #pragma unroll
-        for (int q = 0; q < kReduceSlots; ++q) fold<R>(acc[q], pend[q]);
+        for (int q = 0; q < kReduceSlots; ++q) {
+            acc[q] = seg_acc_load<R>(s_acc[q], threadIdx.x);
+            fold<R>(acc[q], pend[q]);
+        }
         if constexpr (sizeof(R) == 4) {
             chunk_reduce(acc, partials + (int64_t)cid * kReduceSlots);
         } else {

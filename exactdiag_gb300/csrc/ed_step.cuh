@@ -191,74 +191,108 @@ constexpr int kExpandThreads = 256;
 // out[r] = conj(u^e) x[rep] / sqrt(orbit) for every spin configuration r of each task's block, as
 // the stabiliser rows' exchange terms read it (resolve_cand, bitmap_row and the phase rule of
 // gather_add, applied once per configuration instead of once per row and bond); 0 where the
-// sector's phases exclude the configuration.
+// sector's phases exclude the configuration.  A warp takes 32 runs of kExpandRun consecutive ranks
+// (one per lane: one unrank, then next-combination steps); for vectors of at most 8 bytes the
+// values go through shared memory so that the warp's stores are contiguous (the runs of a task
+// follow one another), else each lane stores its own run.
 template <typename R, bool CPLX>
 __global__ void __launch_bounds__(kExpandThreads)
     expand_cand_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                        const ExpandTask* __restrict__ tasks, int ntasks, int64_t n_spin, void* v, void* xfull) {
+    using T = typename Vec<R, CPLX>::T;
+    constexpr bool kStage = sizeof(T) <= 8;
+    constexpr int kW = kExpandThreads / 32;
+    // [warp][position in the run][lane, padded]: a lane's writes and the warp's reads stay within
+    // two-way bank conflicts
+    __shared__ T s_stage[kStage ? kW : 1][kExpandRun][kStage ? 33 : 1];
     extern __shared__ __align__(16) uint8_t smem[];
     const HvTables<R> tb = load_tables<R>(views[0], smem);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t runs = (n_spin + kExpandRun - 1) / kExpandRun;
     const int64_t total = runs * ntasks;
-    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
-        const int t = (int)(u / runs);
-        const int64_t r0 = (u - (int64_t)t * runs) * kExpandRun;
-        const int64_t r1 = r0 + kExpandRun < n_spin ? r0 + kExpandRun : n_spin;
-        const ExpandTask T = tasks[t];
-        const SectorView& S = views[T.sec];
-        const BlockDesc* D = S.desc + T.block;
-        const int ncand = D->ncand;
-        const int64_t word_off = D->word_off;
-        const void* x = vec_at<R, CPLX>(v, offs[T.sec]);
-        void* out = vec_at<R, CPLX>(xfull, T.out_off);
-        uint32_t cfg = colex_unrank(r0, S.Ns, S.Nd, tb.comb);
-        // kExpandBatch configurations at a time: their bitmap words, then their x, are in flight together
-        for (int64_t r = r0; r < r1; r += kExpandBatch) {
-            CandResult c[kExpandBatch];
-            uint32_t rk[kExpandBatch];
-            bool live[kExpandBatch];
+    const int64_t nwarps = (int64_t)gridDim.x * kW;
+    for (int64_t wi = (int64_t)blockIdx.x * kW + warp; wi * 32 < total; wi += nwarps) {
+        const int64_t u = wi * 32 + lane;
+        T* dst = nullptr;  // this lane's run in the output
+        int len = 0;
+        if (u < total) {
+            const int t = (int)(u / runs);
+            const int64_t r0 = (u - (int64_t)t * runs) * kExpandRun;
+            const int64_t r1 = r0 + kExpandRun < n_spin ? r0 + kExpandRun : n_spin;
+            const ExpandTask T_ = tasks[t];
+            const SectorView& S = views[T_.sec];
+            const BlockDesc* D = S.desc + T_.block;
+            const int ncand = D->ncand;
+            const int64_t word_off = D->word_off;
+            const void* x = vec_at<R, CPLX>(v, offs[T_.sec]);
+            dst = reinterpret_cast<T*>(xfull) + T_.out_off + r0;
+            len = (int)(r1 - r0);
+            uint32_t cfg = colex_unrank(r0, S.Ns, S.Nd, tb.comb);
+            // kExpandBatch configurations at a time: their bitmap words, then their x, are in flight together
+            for (int64_t r = r0; r < r1; r += kExpandBatch) {
+                CandResult c[kExpandBatch];
+                uint32_t rk[kExpandBatch];
+                bool live[kExpandBatch];
 #pragma unroll
-            for (int u = 0; u < kExpandBatch; ++u) {
-                live[u] = false;
-                rk[u] = 0;
-                c[u] = CandResult{0u, 1, 0, false};
-                if (r + u < r1) {
-                    c[u] = resolve_cand<true>(D->cand, ncand, cfg, S.Ns);
-                    live[u] = c[u].valid;
-                    if (live[u]) rk[u] = spin_rank(c[u].best, tb.rank, S.Nd);
-                    if (r + u + 1 < r1) cfg = next_combination(cfg);
+                for (int q = 0; q < kExpandBatch; ++q) {
+                    live[q] = false;
+                    rk[q] = 0;
+                    c[q] = CandResult{0u, 1, 0, false};
+                    if (r + q < r1) {
+                        c[q] = resolve_cand<true>(D->cand, ncand, cfg, S.Ns);
+                        live[q] = c[q].valid;
+                        if (live[q]) rk[q] = spin_rank(c[q].best, tb.rank, S.Nd);
+                        if (r + q + 1 < r1) cfg = next_combination(cfg);
+                    }
                 }
-            }
-            ulonglong2 bp[kExpandBatch];
+                ulonglong2 bp[kExpandBatch];
 #pragma unroll
-            for (int u = 0; u < kExpandBatch; ++u)
-                if (live[u]) bp[u] = S.bitpref[word_off + (rk[u] >> 6)];
-            R xr[kExpandBatch], xi[kExpandBatch];
+                for (int q = 0; q < kExpandBatch; ++q)
+                    if (live[q]) bp[q] = S.bitpref[word_off + (rk[q] >> 6)];
+                R xr[kExpandBatch], xi[kExpandBatch];
 #pragma unroll
-            for (int u = 0; u < kExpandBatch; ++u) {
-                xr[u] = xi[u] = R(0);
-                if (live[u]) {
-                    const uint64_t bit = 1ull << (rk[u] & 63u);
-                    if (bp[u].x & bit) {
-                        const int64_t j = (int64_t)bp[u].y + __popcll(bp[u].x & (bit - 1ull));
-                        ld<R, CPLX>(x, j, xr[u], xi[u]);
+                for (int q = 0; q < kExpandBatch; ++q) {
+                    xr[q] = xi[q] = R(0);
+                    if (live[q]) {
+                        const uint64_t bit = 1ull << (rk[q] & 63u);
+                        if (bp[q].x & bit) {
+                            const int64_t j = (int64_t)bp[q].y + __popcll(bp[q].x & (bit - 1ull));
+                            ld<R, CPLX>(x, j, xr[q], xi[q]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kExpandBatch; ++q) {
+                    if (r + q >= r1) continue;
+                    const R f = tb.rsqrtv[orbit_of_count(S.N, c[q].count)];
+                    R vr, vi = R(0);
+                    if constexpr (CPLX) {
+                        const R pr = f * tb.cosv[c[q].e], pi = f * tb.sinv[c[q].e];
+                        vr = pr * xr[q] - pi * xi[q];
+                        vi = pr * xi[q] + pi * xr[q];
+                    } else {
+                        vr = (c[q].e == 0 ? f : -f) * xr[q];
+                    }
+                    if constexpr (kStage) {
+                        if constexpr (CPLX) s_stage[warp][r + q - r0][lane] = T{vr, vi};
+                        else s_stage[warp][r + q - r0][lane] = vr;
+                    } else {
+                        st<R, CPLX>(dst, r + q - r0, vr, vi);
                     }
                 }
             }
-#pragma unroll
-            for (int u = 0; u < kExpandBatch; ++u) {
-                if (r + u >= r1) continue;
-                const R f = tb.rsqrtv[orbit_of_count(S.N, c[u].count)];
-                R vr, vi = R(0);
-                if constexpr (CPLX) {
-                    const R pr = f * tb.cosv[c[u].e], pi = f * tb.sinv[c[u].e];
-                    vr = pr * xr[u] - pi * xi[u];
-                    vi = pr * xi[u] + pi * xr[u];
-                } else {
-                    vr = (c[u].e == 0 ? f : -f) * xr[u];
-                }
-                st<R, CPLX>(out, r + u, vr, vi);
+        }
+        if constexpr (kStage) {
+            // element e of the warp's 32 runs: run e / kExpandRun, position e % kExpandRun
+            __syncwarp();
+#pragma unroll 4
+            for (int j = 0; j < kExpandRun; ++j) {
+                const int e = j * 32 + lane, src = e / kExpandRun, pos = e % kExpandRun;
+                T* const d = reinterpret_cast<T*>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(dst), src));
+                const int n = __shfl_sync(0xffffffffu, len, src);
+                if (pos < n) d[pos] = s_stage[warp][pos][src];
             }
+            __syncwarp();  // the stage is read before the warp's next runs write it
         }
     }
 }
@@ -268,7 +302,15 @@ inline int launch_expand(const StepArgs& a, cudaStream_t st, int num_sms) {
     auto* kern = expand_cand_kernel<R, CPLX>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.smem);
     const int64_t work = ((a.n_spin + kExpandRun - 1) / kExpandRun) * a.ntasks;
-    const int grid = grid_for(work, kExpandThreads, num_sms, 4);
+    // every CTA loops over the work: launch no more than fit at once (a second, partial wave would
+    // leave most SMs idle)
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kExpandThreads, a.smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    const int grid = grid_for(work, kExpandThreads, num_sms, per_sm < 4 ? per_sm : 4);
     kern<<<grid, kExpandThreads, a.smem, st>>>(a.views, a.offs, a.tasks, a.ntasks, a.n_spin, a.v, a.xfull);
     ED_CHECK_LAUNCH("expand_cand_kernel");
     return ED_OK;

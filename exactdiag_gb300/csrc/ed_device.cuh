@@ -313,6 +313,23 @@ __device__ __forceinline__ CandResult resolve_cand(const CandParams* c, int nc, 
     return r;
 }
 
+// resolve_cand<true> over candidates held in registers (nc <= kMaxCand): the same rule, the same result.
+__device__ __forceinline__ CandResult resolve_cand_held(const CandParams (&c)[kMaxCand], int nc, uint32_t x, int Ns) {
+    CandResult r{x, 1, c[0].e, true};
+#pragma unroll
+    for (int k = 1; k < kMaxCand; ++k) {
+        if (k >= nc) break;
+        const uint32_t img = cand_image(c[k], x, Ns);
+        if (img < r.best) {
+            r = {img, 1, c[k].e, true};
+        } else if (img == r.best) {
+            ++r.count;
+            if (c[k].e != r.e) r.valid = false;
+        }
+    }
+    return r;
+}
+
 __device__ __forceinline__ int64_t bitmap_row(const SectorView& S, int64_t word_off, uint32_t r) {
     const ulonglong2 bp = S.bitpref[word_off + (r >> 6)];
     const uint64_t bit = 1ull << (r & 63u);

@@ -228,6 +228,57 @@ __global__ void __launch_bounds__(kExpandThreads)
             dst = reinterpret_cast<T*>(xfull) + T_.out_off + r0;
             len = (int)(r1 - r0);
             uint32_t cfg = colex_unrank(r0, S.Ns, S.Nd, tb.comb);
+            if (len == kExpandRun) {
+                // a full run (all but a block's last): the same resolution and values without per-entry
+                // branches -- every bitmap word and x load is issued (a configuration that is not a
+                // row reads x[0] and takes zero), the candidates are held in registers
+                CandParams cp[kMaxCand];
+#pragma unroll
+                for (int k = 0; k < kMaxCand; ++k) cp[k] = k < ncand ? D->cand[k] : D->cand[0];
+                const ulonglong2* __restrict__ bw = S.bitpref + word_off;
+#pragma unroll 1
+                for (int q0 = 0; q0 < kExpandRun; q0 += kExpandBatch) {
+                    CandResult c[kExpandBatch];
+                    uint32_t rk[kExpandBatch];
+#pragma unroll
+                    for (int q = 0; q < kExpandBatch; ++q) {
+                        c[q] = resolve_cand_held(cp, ncand, cfg, S.Ns);
+                        rk[q] = spin_rank(c[q].best, tb.rank, S.Nd);
+                        cfg = next_combination(cfg);  // past the run's last entry: unused
+                    }
+                    ulonglong2 bp[kExpandBatch];
+#pragma unroll
+                    for (int q = 0; q < kExpandBatch; ++q) bp[q] = bw[rk[q] >> 6];
+                    R xr[kExpandBatch], xi[kExpandBatch];
+                    bool hit[kExpandBatch];
+#pragma unroll
+                    for (int q = 0; q < kExpandBatch; ++q) {
+                        const uint64_t bit = 1ull << (rk[q] & 63u);
+                        hit[q] = c[q].valid && (bp[q].x & bit) != 0ull;
+                        const int64_t j = hit[q] ? (int64_t)bp[q].y + __popcll(bp[q].x & (bit - 1ull)) : 0;
+                        ld<R, CPLX>(x, j, xr[q], xi[q]);
+                        if (!hit[q]) xr[q] = xi[q] = R(0);  // as the general path: the product of zero
+                    }
+#pragma unroll
+                    for (int q = 0; q < kExpandBatch; ++q) {
+                        const R f = tb.rsqrtv[orbit_of_count(S.N, c[q].count)];
+                        R vr, vi = R(0);
+                        if constexpr (CPLX) {
+                            const R pr = f * tb.cosv[c[q].e], pi = f * tb.sinv[c[q].e];
+                            vr = pr * xr[q] - pi * xi[q];
+                            vi = pr * xi[q] + pi * xr[q];
+                        } else {
+                            vr = (c[q].e == 0 ? f : -f) * xr[q];
+                        }
+                        if constexpr (kStage) {
+                            if constexpr (CPLX) s_stage[warp][q0 + q][lane] = T{vr, vi};
+                            else s_stage[warp][q0 + q][lane] = vr;
+                        } else {
+                            st<R, CPLX>(dst, q0 + q, vr, vi);
+                        }
+                    }
+                }
+            } else
             // kExpandBatch configurations at a time: their bitmap words, then their x, are in flight together
             for (int64_t r = r0; r < r1; r += kExpandBatch) {
                 CandResult c[kExpandBatch];

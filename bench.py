@@ -48,7 +48,7 @@ UNIT = "Lanczos steps/s"
 SECTOR = (14, 2, 13, 0, 0)
 WEIGHTS = {"tl": 1.0, "tr": 1.0, "jl": 0.5, "jr": 0.5}
 # the kernel generation the committed ncu traffic summary was captured on
-KERNEL_VERSION = "seg_step_kernel v8"
+KERNEL_VERSION = "seg_step_kernel v9"
 TRAFFIC_FILE = ROOT / "profiles" / "seg_step_2x14_traffic.txt"
 
 

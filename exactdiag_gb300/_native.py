@@ -38,6 +38,8 @@ SIGNATURES = {
     "ed_sector_get_launch": (_c.c_int, [_vp, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
     "ed_sector_set_step_shape": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.c_int]),
     "ed_sector_get_step_shape": (_c.c_int, [_vp, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    "ed_sector_set_segment_window": (_c.c_int, [_vp, _c.c_int]),
+    "ed_sector_get_segment_window": (_c.c_int, [_vp, _c.POINTER(_c.c_int)]),
     "ed_sector_row_kinds": (_c.c_int, [_vp, _c.POINTER(_c.c_int)]),
     "ed_sector_kind_rows": (_c.c_int, [_vp, _c.POINTER(_c.c_int64)]),
     "ed_sector_step_launches": (_c.c_int, [_vp, _c.POINTER(_c.c_int)]),

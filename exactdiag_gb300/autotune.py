@@ -7,9 +7,10 @@ candidate and keeps the fastest, in two stages:
    x rows per lane worked on together, and the variant whose gathers go through shared memory
    (ed_sector_set_step_shape) -- these change only how work maps onto threads and CTAs, never a
    result bit;
-2. for the winner, the rows of a segment chunk (the unit of work and of the step's partial sums):
-   the sector is re-planned for each candidate, so its recursions' last bits follow the choice (the
-   same for a sector alone and in a batch, which both apply it).
+2. for the winner, the offsets of a segment chunk's window (32: a lane's two rows in two segments;
+   64: in one segment) x the rows of a segment chunk (the unit of work and of the step's partial
+   sums): the sector is re-planned for each candidate, so its recursions' last bits follow the choice
+   (the same for a sector alone and in a batch, which both apply it).
 
 Results are cached as JSON keyed by GPU name and shape, so later runs apply the choice without
 timing.  Cache file: $EXACTDIAG_GB300_AUTOTUNE, else ~/.cache/exactdiag_gb300/autotune.json.
@@ -34,6 +35,8 @@ ROWS_PER_LANE = (1, 2)
 STAGED_CANDIDATES = ((2, 0, 1), (2, 0, 2))  # (register variant, CTAs per SM, rows per lane)
 CHUNK_ROWS = (2048, 4096, 8192, 16384, 32768)
 DEFAULT_CHUNK_ROWS = 16384
+WINDOWS = (32, 64)  # offsets of a segment chunk's window (64: not with staged gathers)
+DEFAULT_WINDOW = 32
 
 
 def cache_path() -> pathlib.Path:
@@ -85,11 +88,23 @@ def get_step_shape(sector: DeviceSector) -> tuple[int, int, int]:
     return a.value, c.value, g.value
 
 
+def set_window(sector: DeviceSector, offsets: int) -> None:
+    nat.check("ed_sector_set_segment_window", sector._lib.ed_sector_set_segment_window(sector.handle, int(offsets)))
+
+
+def get_window(sector: DeviceSector) -> int:
+    w = ctypes.c_int()
+    nat.check("ed_sector_get_segment_window", sector._lib.ed_sector_get_segment_window(sector.handle, ctypes.byref(w)))
+    return w.value
+
+
 def apply(sector: DeviceSector, rec: dict) -> None:
     """Set a tuned record's launch and work shape on a sector."""
     set_launch(sector, rec["min_ctas_per_sm"], rec["ctas_per_sm"])
+    set_window(sector, DEFAULT_WINDOW)  # staged gathers need it; a 64-offset record is never staged
     set_step_shape(sector, rec.get("rows_per_lane", 0), rec.get("chunk_rows", DEFAULT_CHUNK_ROWS),
                    rec.get("staged", 0))
+    set_window(sector, rec.get("window", DEFAULT_WINDOW))
 
 
 def get_launch(sector: DeviceSector) -> tuple[int, int]:
@@ -152,7 +167,7 @@ def tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int = 3, use_
 def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cache: bool) -> dict:
     key = _key(sector, dtype)
     cache = _load() if use_cache else {}
-    if key in cache and "staged" in cache[key]:
+    if key in cache and "window" in cache[key]:
         rec = cache[key]
         apply(sector, rec)
         return dict(rec, cached=True)
@@ -176,6 +191,7 @@ def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cac
         return start.elapsed_time(stop) / steps
 
     timings = {}
+    set_window(sector, DEFAULT_WINDOW)
     set_step_shape(sector, 0, DEFAULT_CHUNK_ROWS)
     shapes = [(minb, ctas, nr, 0) for minb, ctas in CANDIDATES for nr in ROWS_PER_LANE]
     shapes += [(minb, ctas, nr, 1) for minb, ctas, nr in STAGED_CANDIDATES]
@@ -185,21 +201,27 @@ def _tune(sector: DeviceSector, weights, dtype: torch.dtype, steps: int, use_cac
             set_step_shape(sector, nr, DEFAULT_CHUNK_ROWS, staged)
         except nat.EngineError:
             continue
-        timings[(minb, ctas, nr, staged, DEFAULT_CHUNK_ROWS)] = time_steps()
+        timings[(minb, ctas, nr, staged, DEFAULT_WINDOW, DEFAULT_CHUNK_ROWS)] = time_steps()
     best = min(timings, key=timings.get)
     set_launch(sector, best[0], best[1])
-    for rows in CHUNK_ROWS:
-        if rows == DEFAULT_CHUNK_ROWS:
-            continue
-        set_step_shape(sector, best[2], rows, best[3])
-        timings[(best[0], best[1], best[2], best[3], rows)] = time_steps()
+    set_step_shape(sector, best[2], DEFAULT_CHUNK_ROWS, best[3])
+    for win in WINDOWS:
+        if win != DEFAULT_WINDOW and best[3]:
+            continue  # staged gathers: 32-offset windows only
+        set_window(sector, win)
+        for rows in CHUNK_ROWS:
+            if (win, rows) == (DEFAULT_WINDOW, DEFAULT_CHUNK_ROWS):
+                continue
+            set_step_shape(sector, best[2], rows, best[3])
+            timings[(best[0], best[1], best[2], best[3], win, rows)] = time_steps()
+        set_window(sector, DEFAULT_WINDOW)
     best = min(timings, key=timings.get)
-    set_launch(sector, best[0], best[1])
-    set_step_shape(sector, best[2], best[4], best[3])
     rec = {"min_ctas_per_sm": best[0], "ctas_per_sm": best[1], "rows_per_lane": best[2], "staged": best[3],
-           "chunk_rows": best[4], "ms_per_step": timings[best], "grid": get_launch(sector)[1],
+           "window": best[4], "chunk_rows": best[5], "ms_per_step": timings[best],
            "candidates": {",".join(str(v) for v in k): t for k, t in timings.items()},
-           "candidate_key": "min_ctas_per_sm,ctas_per_sm,rows_per_lane,staged,chunk_rows"}
+           "candidate_key": "min_ctas_per_sm,ctas_per_sm,rows_per_lane,staged,window,chunk_rows"}
+    apply(sector, rec)
+    rec["grid"] = get_launch(sector)[1]
     cache[key] = rec
     if use_cache:
         _save(cache)

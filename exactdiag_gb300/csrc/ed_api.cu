@@ -153,6 +153,17 @@ int ed_sector_set_step_shape(ed_sector* h, int rows_per_lane, int chunk_rows, in
     return set_step_shape(h->s, rows_per_lane, chunk_rows, staged_gathers);
 }
 
+int ed_sector_set_segment_window(ed_sector* h, int offsets) {
+    if (!h) return set_error(ED_ERR_INVALID, "ed_sector_set_segment_window: NULL sector");
+    return set_segment_window(h->s, offsets);
+}
+
+int ed_sector_get_segment_window(const ed_sector* h, int* offsets) {
+    if (!h || !offsets) return set_error(ED_ERR_INVALID, "ed_sector_get_segment_window: NULL argument");
+    *offsets = h->s.seg_win;
+    return ED_OK;
+}
+
 int ed_sector_get_step_shape(const ed_sector* h, int* rows_per_lane, int* chunk_rows, int* staged_gathers) {
     if (!h || !rows_per_lane || !chunk_rows || !staged_gathers)
         return set_error(ED_ERR_INVALID, "ed_sector_get_step_shape: NULL argument");
@@ -192,7 +203,7 @@ int ed_singlet_correlations(const ed_sector* h, int dtype, const void* psi_dev, 
 int ed_sector_row_kinds(const ed_sector* h, int counts[3]) {
     if (!h || !counts) return set_error(ED_ERR_INVALID, "ed_sector_row_kinds: NULL argument");
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_row_kinds: basis not built");
-    counts[0] = h->s.kind_count[kRowsFree];
+    counts[0] = h->s.kind_count[kRowsFree] + h->s.kind_count[kRowsFree64];
     counts[1] = h->s.kind_count[kRowsCand];
     counts[2] = h->s.kind_count[kRowsGeneric];
     return ED_OK;
@@ -203,7 +214,7 @@ int ed_sector_step_launches(const ed_sector* h, int* launches) {
     if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_sector_step_launches: basis not built");
     const Sector& s = h->s;
     int n = s.n_tasks > 0 ? 1 : 0;  // expanded copies
-    for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind) n += s.kind_count[kind] > 0 ? 1 : 0;
+    for (int kind = kRowsFree64; kind <= kRowsGeneric; ++kind) n += s.kind_count[kind] > 0 ? 1 : 0;
     *launches = n + 1 + 4;  // + scalars; update: flat pass, exact-norm pass, exact b, scaling pass
     return ED_OK;
 }

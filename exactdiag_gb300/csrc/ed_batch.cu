@@ -336,9 +336,10 @@ __global__ void __launch_bounds__(kUpdThreads, 4)
 // Chunks of every sector.  Row chunks: each block's rows cut every chunk_rows[kind] (a chunk never
 // straddles two blocks), sector-major in row order; a kind's chunks are kChunkRows long, halved (down
 // to kChunkRows / 8) while the sector's rows of that kind would make fewer chunks than four per SM.
-// H.v chunks: for a free block, its segments class by class (kl = 0 .. P), seg_chunk_rows / kSegWin
-// segments per range (whole rounds of the CTA's warps, two segments per warp), each range window by
-// window (kSegWin offsets of every segment); for the other blocks, their row chunks.
+// H.v chunks: for a free block, its segments class by class (kl = 0 .. P), seg_chunk_rows / seg_win
+// segments per range (whole rounds of the CTA's warps: two segments per warp with 32-offset windows,
+// one with 64), each range window by window (seg_win offsets of every segment; listed as kRowsFree
+// or, with 64-offset windows, kRowsFree64); for the other blocks, their row chunks.
 // Both depend on the sector alone: a sector is cut the same way alone and in a batch, so its
 // per-chunk sums, and with them its recursion, are the same bits either way.  Expanded copies: one
 // per block of Sector::copy_blocks, sector by sector.
@@ -402,8 +403,9 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
                 if (nseg <= 0) continue;
                 int64_t nA = 1;  // C(Pb, kl)
                 for (int j = 1; j <= kl; ++j) nA = nA * (Pb - kl + j) / j;
-                const int64_t windows = (nA + kSegWin - 1) / kSegWin;
-                const int64_t per = 2 * warps * std::max<int64_t>(1, S.seg_chunk_rows / (2 * warps * kSegWin));
+                const int64_t sw = S.seg_win, spw = sw == 32 ? 2 : 1;  // offsets per window, segments per warp
+                const int64_t windows = (nA + sw - 1) / sw;
+                const int64_t per = spw * warps * std::max<int64_t>(1, S.seg_chunk_rows / (spw * warps * sw));
                 for (int64_t g = 0; g < nseg; g += per)
                     for (int64_t pc = 0; pc < windows; ++pc) {
                         BatchChunk c{};
@@ -414,7 +416,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
                         c.xoff = copy_base;
                         c.kl = kl;
                         c.piece = (int32_t)pc;
-                        by_kind[kRowsFree].push_back((int)P.hv.size());
+                        by_kind[S.seg_win == 32 ? kRowsFree : kRowsFree64].push_back((int)P.hv.size());
                         P.hv.push_back(c);
                     }
             }
@@ -425,7 +427,7 @@ void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& P) {
         P.ccount[s] = (int)P.chunks.size() - P.cfirst[s];
         P.hv_count[s] = (int)P.hv.size() - P.hv_first[s];
     }
-    for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind) {
+    for (int kind = kRowsFree64; kind <= kRowsGeneric; ++kind) {
         P.kind_first[kind] = (int)P.kind_idx.size();
         P.kind_count[kind] = (int)by_kind[kind].size();
         P.kind_idx.insert(P.kind_idx.end(), by_kind[kind].begin(), by_kind[kind].end());
@@ -444,7 +446,10 @@ static int step_hv_all(int dtype, int minb, int nr, int staged, int free_grid, i
     a.idx = idx0 + kind_first[kRowsFree];
     a.count = kind_count[kRowsFree];
     a.grid = free_grid;
-    if (int rc = step_hv_free(dtype, minb, nr, staged, a, st)) return rc;
+    if (int rc = step_hv_free(dtype, minb, nr, staged, 1, a, st)) return rc;
+    a.idx = idx0 + kind_first[kRowsFree64];
+    a.count = kind_count[kRowsFree64];
+    if (int rc = step_hv_free(dtype, minb, nr, 0, 0, a, st)) return rc;
     a.idx = idx0 + kind_first[kRowsCand];
     a.count = kind_count[kRowsCand];
     a.grid = dtype == ED_F32 ? cand_grid_f32 : other_grid;
@@ -470,6 +475,7 @@ namespace {
 struct BatchWorkspace {
     std::vector<uint64_t> serials;
     std::vector<int> chunk_rows;  // each sector's segment chunk length (its plan)
+    std::vector<int> wins;        // each sector's segment window (its plan)
     int device = -1, dtype = -1, m = 0, use_graph = 0, nr = 0, staged = 0;
     HvWeights w{};
     int minb = 0, hv_grid = 0, other_grid = 0, cand_grid = 0;
@@ -496,7 +502,8 @@ struct BatchWorkspace {
         if (dev != device || dt != dtype || mm != m || graph != use_graph || secs.size() != serials.size())
             return false;
         for (size_t i = 0; i < secs.size(); ++i)
-            if (secs[i]->serial != serials[i] || secs[i]->seg_chunk_rows != chunk_rows[i]) return false;
+            if (secs[i]->serial != serials[i] || secs[i]->seg_chunk_rows != chunk_rows[i] || secs[i]->seg_win != wins[i])
+                return false;
         for (int t = 0; t < 4; ++t)
             if (ww.w[t] != w.w[t]) return false;
         const Sector& s0 = *secs[0];
@@ -641,6 +648,7 @@ static int batch_typed(const std::vector<const Sector*>& secs, const HvWeights& 
         for (const Sector* s : secs) {
             W->serials.push_back(s->serial);
             W->chunk_rows.push_back(s->seg_chunk_rows);
+            W->wins.push_back(s->seg_win);
         }
         int rc = batch_prepare<R, CPLX>(*W, secs, m, st);
         if (rc == ED_OK && use_graph) {
@@ -801,12 +809,26 @@ int set_launch(Sector& s, int minb, int ctas_per_sm) {
 int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows, int staged) {
     if (rows_per_lane < 0 || rows_per_lane > 2) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: rows per lane");
     if (staged != 0 && staged != 1) return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: staged must be 0 or 1");
+    if (staged && s.seg_win != 32)
+        return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: staged gathers need 32-offset segment windows");
     if (chunk_rows < 1024 || chunk_rows > 65536 || (chunk_rows & (chunk_rows - 1)))
         return set_error(ED_ERR_INVALID, "ed_sector_set_step_shape: chunk rows must be a power of two in [1024, 65536]");
     s.seg_nr = rows_per_lane;
     s.seg_staged = staged;
     if (chunk_rows == s.seg_chunk_rows) return ED_OK;
     s.seg_chunk_rows = chunk_rows;
+    return s.built ? single_setup(s) : ED_OK;
+}
+
+// The offsets of a segment chunk's window, 32 or 64 (a new value re-plans the sector, like a new chunk
+// length).  64 cannot go with staged gathers.
+int set_segment_window(Sector& s, int offsets) {
+    if (offsets != 32 && offsets != 64)
+        return set_error(ED_ERR_INVALID, "ed_sector_set_segment_window: offsets must be 32 or 64");
+    if (offsets == 64 && s.seg_staged)
+        return set_error(ED_ERR_INVALID, "ed_sector_set_segment_window: staged gathers need 32-offset windows");
+    if (offsets == s.seg_win) return ED_OK;
+    s.seg_win = offsets;
     return s.built ? single_setup(s) : ED_OK;
 }
 

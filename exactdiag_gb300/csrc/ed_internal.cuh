@@ -72,10 +72,11 @@ constexpr int kChunkRows = 8192;
 // chunk of it holds.
 constexpr int kSegThreads = 256;
 constexpr int kSegChunkRows = 16384;
-constexpr int kSegWin = 32;  // offsets of a segment a segment chunk covers (one per lane, in two segments at a time)
+constexpr int kSegWin = 32;  // default offsets of a segment a segment chunk covers (Sector::seg_win: 32 or 64)
 
 // Row kinds of the fused step: each kind has its own kernel (and register budget).
 enum RowKind : int {
+    kRowsFree64 = 0,   // blocks with a trivial stabiliser, planned with 64-offset windows (Sector::seg_win)
     kRowsFree = 1,     // blocks with a trivial stabiliser: colex deltas, no orbit lookups
     kRowsCand = 2,     // blocks with a small stabiliser: coset candidates and bitmap lookups
     kRowsGeneric = 3,  // everything else (and sectors without descriptors): the orbit walk
@@ -139,6 +140,9 @@ struct Sector {
     int seg_nr = 0;              // rows per lane the free-row kernel works on together (0: by dtype)
     int seg_staged = 0;          // 1: the free-row kernel gathers through shared memory (cp.async)
     int seg_chunk_rows = kSegChunkRows;  // rows of a segment chunk (the plan's unit of work and of partial sums)
+    // offsets of a segment chunk's window: 32 (a lane's two rows in two segments at the same offset)
+    // or 64 (a lane's two rows 32 offsets apart in one segment); part of the plan, like the chunk rows
+    int seg_win = kSegWin;
     int other_grid = 0;          // grid of the other row kinds' step kernels
     int cand_grid_f32 = 0;       // grid of the stabiliser-row kernel for real FP32 vectors
     std::vector<BlockSpan> spans;  // host copy of the blocks' row ranges and kinds
@@ -246,6 +250,7 @@ int build_descriptors(Sector& s);
 int seg_records_build(Sector& s, const std::vector<int>& free_blocks, int64_t nseg);  // ed_segrec.cu
 int set_launch(Sector& s, int minb, int ctas_per_sm);
 int set_step_shape(Sector& s, int rows_per_lane, int chunk_rows, int staged);  // re-plans when chunk_rows changes
+int set_segment_window(Sector& s, int offsets);  // 32 or 64; re-plans when it changes
 void plan_chunks(const std::vector<const Sector*>& secs, ChunkPlan& plan);
 
 // ed_step_free.cu / ed_step_rest.cu: the fused step kernel of one row kind over a list of chunks
@@ -272,10 +277,12 @@ struct StepArgs {
     int64_t n_spin;
     void* xfull;
 };
-int step_hv_free(int dtype, int minb, int nr, int staged, const StepArgs& a, cudaStream_t st);
+// pair: 1 for chunks planned with 32-offset windows (a lane's rows in two segments), 0 for 64-offset
+// windows (kRowsFree64)
+int step_hv_free(int dtype, int minb, int nr, int staged, int pair, const StepArgs& a, cudaStream_t st);
 int step_hv_free_staged(int dtype, int nr, const StepArgs& a, cudaStream_t st);
-int step_hv_free_nr1(int dtype, int minb, const StepArgs& a, cudaStream_t st);
-int step_hv_free_split(int dtype, int nr, const StepArgs& a, cudaStream_t st);
+int step_hv_free_nr1(int dtype, int minb, int pair, const StepArgs& a, cudaStream_t st);
+int step_hv_free_split(int dtype, int nr, int pair, const StepArgs& a, cudaStream_t st);
 // rows per lane of the free-row kernel for a dtype when the sector leaves it open (seg_nr = 0)
 inline int seg_rows_for(int dtype, int nr) { return nr ? nr : ((dtype == ED_F32 || dtype == ED_C64) ? 2 : 1); }
 int step_expand(int dtype, const StepArgs& a, cudaStream_t st);

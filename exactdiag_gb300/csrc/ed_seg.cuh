@@ -262,8 +262,10 @@ __device__ __forceinline__ R seg_slot_ci(const SegSlot<R, CPLX>& S) {
 // own segment's record.  NR = 2 works on the two rows together (their gathers in flight at once);
 // NR = 1 takes them one after the other.  MERGED: rung and leg exchanges share one coefficient
 // (J_rung = J_leg), so each row keeps one exchange sum over one list per bond class; otherwise every
-// element picks its coefficient.
-template <typename R, bool CPLX, int MINB, bool MERGED, int NR, bool STAGED = false>
+// element picks its coefficient.  PAIR = false: 64-offset windows, warp w taking segments begin + w,
+// + 8, ... and in each the rows at offsets t and t + 32 (one record for both rows, two table
+// columns); the sector's plan says which (Sector::seg_win), and the autotuner picks per sector shape.
+template <typename R, bool CPLX, int MINB, bool MERGED, int NR, bool STAGED = false, bool PAIR = true>
 __global__ void __launch_bounds__(kSegThreads, MINB)
     seg_step_kernel(const SectorView* __restrict__ views, const int64_t* __restrict__ offs,
                     const BatchChunk* __restrict__ chunks, const int* __restrict__ idx, int count, HvWeights W,
@@ -271,6 +273,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     double* __restrict__ partials, void* xfull) {
     using T = typename Vec<R, CPLX>::T;
     constexpr int kWarps = kSegThreads / 32;
+    constexpr int kWin = PAIR ? 32 : 64;     // offsets of a chunk's window (columns of the tables)
+    constexpr int kHalves = kWin / 32;       // table columns per lane
+    constexpr int kSegStep = PAIR ? 2 : 1;   // segments a warp takes at a time
+    static_assert(PAIR || !STAGED, "staged gathers use 32-offset windows");
     constexpr int kCols = 32 * NR;  // staged gathers: columns of a slot (the rows worked on together)
     constexpr int kScap = kSegStageBytes / (kCols * (int)sizeof(T));  // staged slots per pass
     extern __shared__ __align__(16) uint8_t seg_stage_smem[];  // STAGED: kWarps * kSegStageBytes
@@ -282,17 +288,18 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
     // hop slots of the chunk: the kind-0 hops then dummies up to a multiple of four, the same for kind 1
     // (nb 1 or 2); a dummy reads the block's first element with coefficient 0
     __shared__ __align__(16) SegSlot<R, CPLX> s_slot[kSegHopSlots];
-    // per-offset terms of the chunk's window (column = lane = offset - window): a column past the
-    // class's rows repeats column 0, so its reads stay valid
-    __shared__ uint8_t s_al[kSegLowMax][kSegWin];      // partners of the antiparallel bonds below P (rung
-                                                       // first), padded with the offset itself
-    __shared__ uint8_t s_xo[kSegMaxX][kSegWin];        // cross bond c: rank_P(Lo ^ low end) (0 past nX)
-    __shared__ uint16_t s_hc[kSegHopSlots][kSegWin];   // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA
-    __shared__ uint32_t s_lane[kSegWin];               // Lo | lob << 16 (cross-bond low-end spins)
-    __shared__ uint32_t s_cnt[kSegWin];                // nr | nlow << 8 (antiparallel bonds below P)
-    __shared__ int s_maxw;                             // longest low list of the window, in fours
-    // per warp: this pair's and the next pair's records
-    __shared__ __align__(16) uint32_t s_rec[kWarps][2][2][kSegRecMax];
+    // per-offset terms of the chunk's window (column = offset - window, lane + 32 h): a column past
+    // the class's rows repeats one that is a row (its own half's first, else the window's first), so
+    // its reads stay valid
+    __shared__ uint8_t s_al[kSegLowMax][kWin];      // partners of the antiparallel bonds below P (rung
+                                                    // first), padded with the offset itself
+    __shared__ uint8_t s_xo[kSegMaxX][kWin];        // cross bond c: rank_P(Lo ^ low end) (0 past nX)
+    __shared__ uint16_t s_hc[kSegHopSlots][kWin];   // hop slot: rank_P(V) (kind 0) or va | vbi << kSegA
+    __shared__ uint32_t s_lane[kWin];               // Lo | lob << 16 (cross-bond low-end spins)
+    __shared__ uint32_t s_cnt[kWin];                // nr | nlow << 8 (antiparallel bonds below P)
+    __shared__ int s_maxw;                          // longest low list of the window, in fours
+    // per warp: this and the next iteration's records (a pair's two, or one segment's)
+    __shared__ __align__(16) uint32_t s_rec[kWarps][2][kSegStep][kSegRecMax];
     __shared__ R s_acc[kReduceSlots][seg_acc_words(sizeof(R))][kSegThreads];  // per thread: the step's sums
     const int P = views[0].seg_p;
     const uint32_t amask = (1u << P) - 1u;
@@ -325,7 +332,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const int kl = ch.kl, Ns = Sp->Ns, Nd = Sp->Nd, N = Sp->N, L = Sp->L;
         const uint32_t nsmask = 0xffffffffu >> (32 - Ns);
         const int nA = (int)comb[kl * kCombStride + P];
-        const int win = kSegWin * ch.piece;
+        const int win = kWin * ch.piece;
         const int nact = min(32, nA - win);  // lanes with rows
         __syncthreads();  // the previous chunk's rows are done with the shared tables
         {
@@ -340,9 +347,12 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         const T* const xb = x + bstart;
         const int n04 = (n0 + 3) & ~3, n124 = (n12 + 3) & ~3;
         {  // the chunk's tables: hop records, per-offset terms, hop slots
-            // the offset whose terms column `lane` holds: its own, or (past the class's rows) the window's first
-            const int tsrc = win + lane < nA ? win + lane : win;
-            const uint32_t lo_c = s_ut[s_utoff[kl] + tsrc];
+            // the offset whose terms column lane + 32 h holds: its own, or (past the class's rows) the
+            // first half's, or the window's first
+            auto tsrc_of = [&](int h) {
+                const int j = win + lane + 32 * h;
+                return j < nA ? j : (win + lane < nA ? win + lane : win);
+            };
             if (warp == 2 && lane < kMaxHops) {
                 // every hop gets a record: absent hops (and those past nhop) read a valid element with
                 // coefficient 0
@@ -388,41 +398,53 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             } else if (warp == 0) {
                 // bonds below P: the antiparallel ones' partners, rung bonds first, padded with the offset
                 // itself up to the table's length (read in fours, the padding taken back out after the sums)
-                int nr = 0, nlow = 0;
-                const int nAb = s_desc.nA, nAr = s_desc.nAr;
-                for (int i = 0; i < nAb; ++i) {
-                    const uint32_t f = s_desc.fA[i], sb = lo_c & f;
-                    if (sb != 0u && sb != f) {
-                        s_al[nlow++][lane] = s_rt[lo_c ^ f];
-                        if (i < nAr) ++nr;
+                int mx = 0;
+                for (int hh = 0; hh < kHalves; ++hh) {
+                    const int col = lane + 32 * hh, tsrc = tsrc_of(hh);
+                    const uint32_t lo_c = s_ut[s_utoff[kl] + tsrc];
+                    int nr = 0, nlow = 0;
+                    const int nAb = s_desc.nA, nAr = s_desc.nAr;
+                    for (int i = 0; i < nAb; ++i) {
+                        const uint32_t f = s_desc.fA[i], sb = lo_c & f;
+                        if (sb != 0u && sb != f) {
+                            s_al[nlow++][col] = s_rt[lo_c ^ f];
+                            if (i < nAr) ++nr;
+                        }
                     }
+                    for (int q = nlow; q < kSegLowMax; ++q) s_al[q][col] = (uint8_t)tsrc;
+                    mx = max(mx, (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow));
+                    s_cnt[col] = (uint32_t)nr | ((uint32_t)nlow << 8);
                 }
-                for (int q = nlow; q < kSegLowMax; ++q) s_al[q][lane] = (uint8_t)tsrc;
-                const int mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)nlow);
-                s_cnt[lane] = (uint32_t)nr | ((uint32_t)nlow << 8);
                 if (lane == 0) s_maxw = (mx + 3) & ~3;
             } else if (warp == 1) {
                 // bonds across P: the partner's low part and this offset's spin at the low end
-                uint32_t lob = 0;
-                for (int cc = 0; cc < kSegMaxX; ++cc) {
-                    const uint32_t a = s_desc.cX[cc][0];
-                    if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
-                    s_xo[cc][lane] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
+                for (int hh = 0; hh < kHalves; ++hh) {
+                    const int col = lane + 32 * hh;
+                    const uint32_t lo_c = s_ut[s_utoff[kl] + tsrc_of(hh)];
+                    uint32_t lob = 0;
+                    for (int cc = 0; cc < kSegMaxX; ++cc) {
+                        const uint32_t a = s_desc.cX[cc][0];
+                        if (cc < nX) lob |= ((lo_c >> a) & 1u) << cc;
+                        s_xo[cc][col] = cc < nX ? s_rt[lo_c ^ (1u << a)] : (uint8_t)0;
+                    }
+                    s_lane[col] = lo_c | (lob << 16);
                 }
-                s_lane[lane] = lo_c | (lob << 16);
             }
             __syncthreads();
             if (warp != 2) {
                 // hop slots, spread over the other warps
                 for (int sl = warp < 2 ? warp : warp - 1; sl < n04 + n124; sl += kWarps - 1) {
                     const int h = sl < n04 ? (sl < n0 ? sl : -1) : (sl - n04 < n12 ? n0 + sl - n04 : -1);
-                    uint32_t hc = 0;
-                    if (h >= 0 && s_hop[h].kind != 3) {
-                        const SegHop<R, CPLX>& F = s_hop[h];
-                        const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
-                        hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
+                    for (int hh = 0; hh < kHalves; ++hh) {
+                        const uint32_t lo_c = s_ut[s_utoff[kl] + tsrc_of(hh)];
+                        uint32_t hc = 0;
+                        if (h >= 0 && s_hop[h].kind != 3) {
+                            const SegHop<R, CPLX>& F = s_hop[h];
+                            const uint32_t V = seg_perm(lo_c, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
+                            hc = F.nb == 0 ? s_rt[V] : seg_hop_thread(V, amask, F.nb, F.bp0, F.bp1);
+                        }
+                        s_hc[sl][lane + 32 * hh] = (uint16_t)hc;
                     }
-                    s_hc[sl][lane] = (uint16_t)hc;
                 }
             } else if (lane < n04 + n124) {
                 const int sl = lane;
@@ -445,11 +467,26 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         T* const y = reinterpret_cast<T*>(other) + offs[ch.sec] + bstart;
         const T* const yp = first ? nullptr : reinterpret_cast<const T*>(vprev) + offs[ch.sec] + bstart;
         const R beta = first ? R(0) : (R)scal[(int64_t)ch.sec * stride + 2 * k];
-        // this lane's offset (rows in both segments of a pair) and its column of the tables
+        // per row r of an iteration: its column of the tables, its offset (read for every lane: a
+        // valid offset), whether it is a row (PAIR: the pair's second segment decides per iteration)
         const int t = win + lane;
-        const uint32_t lnw = s_lane[lane], cnt = s_cnt[lane];
-        const int nlow = (int)(cnt >> 8), nrl = (int)(cnt & 255u);
-        const T* const xt = xb + t;
+        int col[2], tt[2];
+        bool act[2];
+        uint32_t lnw[2];
+        int nlow[2], nrl[2];
+        const T* xt[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            col[r] = PAIR ? lane : lane + 32 * r;
+            const int to = PAIR ? t : t + 32 * r;
+            act[r] = to < nA;
+            tt[r] = act[r] ? to : t;
+            lnw[r] = s_lane[col[r]];
+            const uint32_t cn = s_cnt[col[r]];
+            nlow[r] = (int)(cn >> 8);
+            nrl[r] = (int)(cn & 255u);
+            xt[r] = xb + tt[r];
+        }
 
         // the step's running sums (float-float for FP32) wait in shared memory between folds: eight
         // registers fewer in the row loop, which lets the 4-CTA variant run without spills
@@ -462,10 +499,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
         // loaded, while this pair is worked on; the active lanes together copy every word of a record
         // (segment indices of a class fit 32 bits: SectorView::seg_off)
         const int gend = (int)ch.end;
-        int g = lane < nact ? (int)ch.begin + 2 * warp : gend;  // lanes without rows skip to the reduction
+        int g = lane < nact ? (int)ch.begin + kSegStep * warp : gend;  // lanes without rows skip to the reduction
         auto copy_pair = [&](int gg, uint32_t* dst) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r)
+            for (int r = 0; r < kSegStep; ++r)
                 if (gg + r < gend)
                     for (int w4 = 4 * lane; w4 < (int)rec_len; w4 += 4 * nact)
                         seg_cp_async16(dst + r * kSegRecMax + w4, rec0 + (uint32_t)(gg + r) * rec_len + w4);
@@ -476,16 +513,16 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             copy_pair(g, s_rec[warp][0][0]);
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
-                base[r] = __ldg(segb + (g + r < gend ? g + r : g));
-                seg_ld<R, CPLX>(xt + base[r], xr[r], xi[r]);
-                if (!first) seg_ld<R, CPLX>(yp + base[r] + t, pr[r], pi[r]);
+                base[r] = (PAIR || r == 0) ? __ldg(segb + (PAIR && g + r < gend ? g + r : g)) : base[0];
+                seg_ld<R, CPLX>(xt[r] + base[r], xr[r], xi[r]);
+                if (!first) seg_ld<R, CPLX>(yp + base[r] + tt[r], pr[r], pi[r]);
             }
         }
         seg_cp_commit();
-        for (int it = 0; g < gend; ++it, g += 2 * kWarps) {
-            const bool act1 = g + 1 < gend;  // the pair's second segment exists (warp-uniform)
-            const uint32_t* const sw[2] = {s_rec[warp][it & 1][0], s_rec[warp][it & 1][act1 ? 1 : 0]};
-            const int gn = g + 2 * kWarps;
+        for (int it = 0; g < gend; ++it, g += kSegStep * kWarps) {
+            const bool act1 = PAIR && g + 1 < gend;  // PAIR: the pair's second segment exists (warp-uniform)
+            const uint32_t* const sw[2] = {s_rec[warp][it & 1][0], s_rec[warp][it & 1][act1 ? kSegStep - 1 : 0]};
+            const int gn = g + kSegStep * kWarps;
             if (gn < gend) copy_pair(gn, s_rec[warp][(it + 1) & 1][0]);
             seg_cp_commit();
             uint32_t nbase[2] = {0u, 0u};
@@ -493,9 +530,9 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
             if (gn < gend) {
 #pragma unroll
                 for (int r = 0; r < 2; ++r) {
-                    nbase[r] = __ldg(segb + (gn + r < gend ? gn + r : gn));
-                    seg_ld<R, CPLX>(xt + nbase[r], nxr[r], nxi[r]);
-                    if (!first) seg_ld<R, CPLX>(yp + nbase[r] + t, npr[r], npi[r]);
+                    nbase[r] = (PAIR || r == 0) ? __ldg(segb + (PAIR && gn + r < gend ? gn + r : gn)) : nbase[0];
+                    seg_ld<R, CPLX>(xt[r] + nbase[r], nxr[r], nxi[r]);
+                    if (!first) seg_ld<R, CPLX>(yp + nbase[r] + tt[r], npr[r], npi[r]);
                 }
             }
             seg_cp_wait<1>();  // this pair's records have arrived (the next pair's may be in flight)
@@ -509,11 +546,11 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                 zb[r] = (int)(w1 & 255u);
                 zbr[r] = (int)((w1 >> 8) & 255u);
                 zb4[r] = (zb[r] + 3) & ~3;
-                xm[r] = ((lnw >> 16) ^ (w1 >> 16)) & xall;  // cross bonds antiparallel in row r
+                xm[r] = ((lnw[r] >> 16) ^ (w1 >> 16)) & xall;  // cross bonds antiparallel in row r
             }
 #pragma unroll
             for (int r0 = 0; r0 < 2; r0 += NR) {
-                if (NR == 1 && r0 == 1 && !act1) break;
+                if (PAIR && NR == 1 && r0 == 1 && !act1) break;
                 // ---- the rows at offset t of segments g + r0 (+ 1): y = H x - beta v_{k-1}
                 const T* xs[NR];
                 R er[NR], ei[NR], lr[NR], li[NR], hr[NR], hi[NR];
@@ -527,24 +564,23 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     for (int q0 = 0; q0 < smax; q0 += 4) {
                         R vr[NR][4], vi[NR][4];
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const uint32_t o = s_al[q0 + u][lane];
+                        for (int u = 0; u < 4; ++u)
 #pragma unroll
-                            for (int r = 0; r < NR; ++r) seg_ld<R, CPLX>(xs[r] + o, vr[r][u], vi[r][u]);
-                        }
+                            for (int r = 0; r < NR; ++r)
+                                seg_ld<R, CPLX>(xs[r] + (uint32_t)s_al[q0 + u][col[r0 + r]], vr[r][u], vi[r][u]);
 #pragma unroll
                         for (int u = 0; u < 4; ++u)
 #pragma unroll
-                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < nrl, vr[r][u], vi[r][u]);
+                            for (int r = 0; r < NR; ++r) seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], q0 + u < nrl[r0 + r], vr[r][u], vi[r][u]);
                     }
                     // exchange bonds at or above P: the partner segments at the same offset, four at a
                     // time; the rows together up to the shorter list, then each row's rest
                     auto high4 = [&](int r, int q0, R (&vr)[4], R (&vi)[4]) {
                         const uint4 pw = *reinterpret_cast<const uint4*>(sw[r0 + r] + 4 + q0);  // 16-byte aligned
-                        seg_ld<R, CPLX>(xt + pw.x, vr[0], vi[0]);
-                        seg_ld<R, CPLX>(xt + pw.y, vr[1], vi[1]);
-                        seg_ld<R, CPLX>(xt + pw.z, vr[2], vi[2]);
-                        seg_ld<R, CPLX>(xt + pw.w, vr[3], vi[3]);
+                        seg_ld<R, CPLX>(xt[r0 + r] + pw.x, vr[0], vi[0]);
+                        seg_ld<R, CPLX>(xt[r0 + r] + pw.y, vr[1], vi[1]);
+                        seg_ld<R, CPLX>(xt[r0 + r] + pw.z, vr[2], vi[2]);
+                        seg_ld<R, CPLX>(xt[r0 + r] + pw.w, vr[3], vi[3]);
                     };
                     const int zc = NR == 2 ? min(zb4[r0], zb4[r0 + NR - 1]) : zb4[r0];
                     for (int q0 = 0; q0 < zc; q0 += 4) {
@@ -572,12 +608,12 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             const int cc = c0 + u;
-                            const uint32_t xoc = s_xo[cc][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
+                                const uint32_t xoc = s_xo[cc][col[r0 + r]];
                                 const uint32_t pw = sw[r0 + r][xo + cc];
                                 const uint32_t on = 0u - ((xm[r0 + r] >> cc) & 1u);  // all ones when antiparallel
-                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)t));
+                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)tt[r0 + r]));
                                 seg_ld<R, CPLX>(xb + o, vr[r][u], vi[r][u]);
                             }
                         }
@@ -593,10 +629,9 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             S[u] = s_slot[h4 + u];
-                            const uint32_t hc = s_hc[h4 + u][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r)
-                                seg_ld<R, CPLX>(S[u].tp + (sw[r0 + r][S[u].off] + hc), vr[r][u], vi[r][u]);
+                                seg_ld<R, CPLX>(S[u].tp + (sw[r0 + r][S[u].off] + s_hc[h4 + u][col[r0 + r]]), vr[r][u], vi[r][u]);
                         }
 #pragma unroll
                         for (int u = 0; u < 4; ++u)
@@ -610,10 +645,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             S[u] = s_slot[h4 + u];
-                            const uint32_t hc = s_hc[h4 + u][lane];
-                            const uint32_t wv = S[u].off + 1u + (hc >> kSegA), va = hc & (kSegLow - 1u);
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
+                                const uint32_t hc = s_hc[h4 + u][col[r0 + r]];
+                                const uint32_t wv = S[u].off + 1u + (hc >> kSegA), va = hc & (kSegLow - 1u);
                                 const uint32_t rr = sw[r0 + r][wv] + s_rt[sw[r0 + r][S[u].off] | va];
                                 seg_ld<R, CPLX>(S[u].tp + rr, vr[r][u], vi[r][u]);
                             }
@@ -635,34 +670,33 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     const int e0 = smax, e1 = e0 + zs, e2 = e1 + nX4, e3 = e2 + n04 + n124;
                     for (int p0 = 0; p0 < e3; p0 += kScap) {
                         const int p1 = min(e3, p0 + kScap);
-                        for (int sl = p0; sl < min(p1, e0); ++sl) {
-                            const uint32_t o = s_al[sl][lane];
+                        for (int sl = p0; sl < min(p1, e0); ++sl)
 #pragma unroll
                             for (int r = 0; r < NR; ++r)
-                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xs[r] + o);
-                        }
+                                seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r,
+                                                     xs[r] + (uint32_t)s_al[sl][col[r0 + r]]);
                         for (int sl = max(p0, e0); sl < min(p1, e1); ++sl)
 #pragma unroll
                             for (int r = 0; r < NR; ++r)
                                 if (sl - e0 < zb4[r0 + r])
-                                    seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xt + sw[r0 + r][4 + sl - e0]);
+                                    seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xt[r0 + r] + sw[r0 + r][4 + sl - e0]);
                         for (int sl = max(p0, e1); sl < min(p1, e2); ++sl) {
                             const int cc = sl - e1;
-                            const uint32_t xoc = s_xo[cc][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
+                                const uint32_t xoc = s_xo[cc][col[r0 + r]];
                                 const uint32_t pw = sw[r0 + r][xo + cc];
                                 const uint32_t on = 0u - ((xm[r0 + r] >> cc) & 1u);  // all ones when antiparallel
-                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)t));
+                                const uint32_t o = (on & (pw + xoc)) | (~on & (base[r0 + r] + (uint32_t)tt[r0 + r]));
                                 seg_cp_async_elem<T>(stg + (sl - p0) * kCols + lane + 32 * r, xb + o);
                             }
                         }
                         for (int sl = max(p0, e2); sl < p1; ++sl) {
                             const int hs = sl - e2;  // hop slot: kind 0 below n04, kind 1 from n04
                             const SegSlot<R, CPLX>& S = s_slot[hs];
-                            const uint32_t hc = s_hc[hs][lane];
 #pragma unroll
                             for (int r = 0; r < NR; ++r) {
+                                const uint32_t hc = s_hc[hs][col[r0 + r]];
                                 const uint32_t w0 = sw[r0 + r][S.off];
                                 const uint32_t rr = hs < n04 ? w0 + hc
                                                              : sw[r0 + r][S.off + 1u + (hc >> kSegA)] +
@@ -679,7 +713,7 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                                 if (sl >= e0 && sl < e1 && sl - e0 >= zb4[r0 + r]) continue;  // past the row's high list
                                 R vr, vi;
                                 seg_ld_shared<R, CPLX>(stg + (sl - p0) * kCols + lane + 32 * r, vr, vi);
-                                const bool rung = sl < e0 ? sl < nrl
+                                const bool rung = sl < e0 ? sl < nrl[r0 + r]
                                                           : (sl < e1 ? sl - e0 < zbr[r0 + r] : sl - e1 < nXr);
                                 seg_add<R, CPLX, MERGED>(er[r], ei[r], lr[r], li[r], rung, vr, vi);
                             }
@@ -701,10 +735,10 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
 #pragma unroll 1
                     for (int hh = n0 + n12; hh < nhop; ++hh) {
                         const SegHop<R, CPLX>& F = s_hop[hh];
-                        const uint32_t V =
-                            seg_perm(lnw & 0xffffu, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap, F.rot, F.nsr, nsmask);
 #pragma unroll
                         for (int r = 0; r < NR; ++r) {
+                            const uint32_t V = seg_perm(lnw[r0 + r] & 0xffffu, F.keep, F.band, F.sl, F.sr, F.p, F.q, F.swap,
+                                                        F.rot, F.nsr, nsmask);
                             const uint32_t rr = spin_rank(sw[r0 + r][s_desc.hop_off[hh]] | V, RT, Nd);
                             R vr, vi;
                             seg_ld<R, CPLX>(F.tp + rr, vr, vi);
@@ -718,28 +752,28 @@ __global__ void __launch_bounds__(kSegThreads, MINB)
                     // the padding read the row itself (in split mode into the leg sum; a parallel cross
                     // bond into its own kind's sum): take it back out; then the diagonal, -J/2 per
                     // antiparallel bond
-                    const int pads = (smax - nlow) + (zb4[rr] - zb[rr]) + __popc(~xm[rr] & x4mask & ~(MERGED ? 0u : xrmask));
+                    const int pads = (smax - nlow[rr]) + (zb4[rr] - zb[rr]) + __popc(~xm[rr] & x4mask & ~(MERGED ? 0u : xrmask));
                     R h_r, h_i;
                     if constexpr (MERGED) {
                         const R e_r = er[r] - (R)pads * xr[rr];
                         const R e_i = CPLX ? ei[r] - (R)pads * xi[rr] : R(0);
-                        const R diag = -wr * (R)(nlow + zb[rr] + __popc(xm[rr]));
+                        const R diag = -wr * (R)(nlow[rr] + zb[rr] + __popc(xm[rr]));
                         h_r = wr * e_r + hr[r] + diag * xr[rr];
                         h_i = CPLX ? wr * e_i + hi[r] + diag * xi[rr] : R(0);
                     } else {
                         const R rpad = (R)__popc(~xm[rr] & xrmask);
                         const R a_r = er[r] - rpad * xr[rr], a_i = CPLX ? ei[r] - rpad * xi[rr] : R(0);
                         const R l_r = lr[r] - (R)pads * xr[rr], l_i = CPLX ? li[r] - (R)pads * xi[rr] : R(0);
-                        const int anr = nrl + zbr[rr] + __popc(xm[rr] & xrmask);
-                        const int anl = (nlow - nrl) + (zb[rr] - zbr[rr]) + __popc(xm[rr] & ~xrmask);
+                        const int anr = nrl[rr] + zbr[rr] + __popc(xm[rr] & xrmask);
+                        const int anl = (nlow[rr] - nrl[rr]) + (zb[rr] - zbr[rr]) + __popc(xm[rr] & ~xrmask);
                         const R diag = -(wr * (R)anr + wl * (R)anl);
                         h_r = wr * a_r + wl * l_r + hr[r] + diag * xr[rr];
                         h_i = CPLX ? wr * a_i + wl * l_i + hi[r] + diag * xi[rr] : R(0);
                     }
-                    if (rr == 0 || act1) {
+                    if (PAIR ? (rr == 0 || act1) : act[rr]) {
                         const R y_r = h_r - beta * pr[rr];
                         const R y_i = CPLX ? h_i - beta * pi[rr] : R(0);
-                        st<R, CPLX>(y, (int64_t)base[rr] + t, y_r, y_i);
+                        st<R, CPLX>(y, (int64_t)base[rr] + tt[rr], y_r, y_i);
                         pend[0] = fma_r(xr[rr], h_r, pend[0]);
                         pend[1] = fma_r(y_r, y_r, pend[1]);
                         pend[2] = fma_r(xr[rr], y_r, pend[2]);

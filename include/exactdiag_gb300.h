@@ -68,10 +68,20 @@ int ed_sector_get_launch(const ed_sector* s, int* min_ctas_per_sm, int* grid);
  * rows per lane do not change results; a new chunk length re-plans the sector, and since the step's
  * partial sums are kept per chunk, its recursions then differ in the last bits (a sector still gives
  * the same bits alone and in a batch).  staged_gathers = 1 sends the free-row kernel's gathers through
- * shared memory (cp.async; results unchanged, at most two CTAs per SM).  ED_ERR_INVALID for values out
- * of range.  Call it between steps: a new chunk length replaces the sector's step tables. */
+ * shared memory (cp.async; results unchanged, at most two CTAs per SM; 32-offset segment windows
+ * only).  ED_ERR_INVALID for values out of range.  Call it between steps: a new chunk length replaces
+ * the sector's step tables. */
 int ed_sector_set_step_shape(ed_sector* s, int rows_per_lane, int chunk_rows, int staged_gathers);
 int ed_sector_get_step_shape(const ed_sector* s, int* rows_per_lane, int* chunk_rows, int* staged_gathers);
+
+/* Offsets of a segment chunk's window (tuning; no reference counterpart): 32 (default; a lane's two
+ * rows lie in two segments at the same offset, which keeps the lanes busier on segments whose length
+ * is not a multiple of 64) or 64 (a lane's two rows lie 32 offsets apart in one segment).  Like a new
+ * chunk length, a new window re-plans the sector and changes the last bits of its recursions (the
+ * same alone and in a batch).  ED_ERR_INVALID for other values, and for 64 while staged gathers are
+ * set.  Call it between steps. */
+int ed_sector_set_segment_window(ed_sector* s, int offsets);
+int ed_sector_get_segment_window(const ed_sector* s, int* offsets);
 
 /* Chunks of the sector's fused step per row kind: counts[0] chunks of rows of blocks with a
  * trivial stabiliser (colex-delta rows), counts[1] chunks of rows of blocks with a small

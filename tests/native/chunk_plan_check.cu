@@ -1,7 +1,7 @@
 // Host check of the step layout (ed_batch.cu: plan_chunks) on synthetic sectors: row chunks tile
 // every sector's rows, never straddle two blocks and follow the per-kind length rule (pinned on two
 // hand-built sectors as well); segment chunks tile every class and offset window of every free block
-// in whole rounds of the CTA's warps; a sector is cut the same way alone and inside a batch (what keeps batched
+// in whole rounds of the CTA's warps, for 32- and 64-offset windows; a sector is cut the same way alone and inside a batch (what keeps batched
 // and sequential recursions bit-identical); every listed block gets one expanded copy, and
 // stabiliser chunks point at their block's copy.  Built with nvcc (the file's kernels are compiled
 // but never launched) and run by tests/test_native_host.py; exits non-zero on any difference.
@@ -15,7 +15,7 @@ namespace ed {
 // the other translation units of the library, not exercised here
 int set_error(int code, const char*) { return code; }
 int set_cuda_error(cudaError_t, const char*) { return ED_ERR_CUDA; }
-int step_hv_free(int, int, int, int, const StepArgs&, cudaStream_t) { return 0; }
+int step_hv_free(int, int, int, int, int, const StepArgs&, cudaStream_t) { return 0; }
 int step_expand(int, const StepArgs&, cudaStream_t) { return 0; }
 int step_hv_cand(int, const StepArgs&, cudaStream_t) { return 0; }
 int step_hv_generic(int, const StepArgs&, cudaStream_t) { return 0; }
@@ -46,6 +46,7 @@ void make_sector(Sector& s, std::mt19937_64& rng, int nblocks, int Ns, int Nd) {
     const uint64_t n_spin = comb[Nd][Ns];
     s.num_sms = 152;
     s.n_spin = n_spin;
+    s.seg_win = rng() % 2 ? 32 : 64;
     s.view.Ns = Ns;
     s.view.Nd = Nd;
     s.view.n_blocks = nblocks;
@@ -181,8 +182,9 @@ int main() {
                 expect(a.kl >= 0 && a.kl <= P && a.xoff == 0, "segment chunk class and copies", trial, c);
                 const int64_t nseg = (int64_t)secs[s].host_seg_off[a.kl + 1] - secs[s].host_seg_off[a.kl];
                 const int64_t nA = binom(P, a.kl);
-                const int64_t pieces = (nA + kSegWin - 1) / kSegWin;
-                const int64_t round = 2 * (kSegThreads / 32);  // two segments per warp
+                const int64_t sw = secs[s].seg_win;
+                const int64_t pieces = (nA + sw - 1) / sw;
+                const int64_t round = (sw == 32 ? 2 : 1) * (kSegThreads / 32);  // segments per round of the warps
                 expect(a.piece >= 0 && a.piece < pieces, "window inside the segment", trial, c);
                 int64_t& next = seg_next[a.block][a.kl * 8 + a.piece];
                 expect(a.begin == next && a.end > a.begin && a.end <= nseg, "segment chunks tile their class", trial, c);
@@ -193,7 +195,7 @@ int main() {
                 if (sp.kind == kRowsFree && sp.count > 0)
                     for (int kl = 0; kl <= P; ++kl) {
                         const int64_t nA = binom(P, kl);
-                        const int64_t pieces = (nA + kSegWin - 1) / kSegWin;
+                        const int64_t pieces = (nA + secs[s].seg_win - 1) / secs[s].seg_win;
                         for (int64_t pc = 0; pc < pieces; ++pc)
                             expect(seg_next[sp.block][kl * 8 + pc] ==
                                        (int64_t)secs[s].host_seg_off[kl + 1] - secs[s].host_seg_off[kl],
@@ -202,12 +204,14 @@ int main() {
         }
         // kind lists: every H.v chunk id once, grouped by kind
         std::vector<int> seen(batch.hv.size(), 0);
-        for (int kind = kRowsFree; kind <= kRowsGeneric; ++kind)
+        for (int kind = kRowsFree64; kind <= kRowsGeneric; ++kind)
             for (int i = 0; i < batch.kind_count[kind]; ++i) {
                 const int id = batch.kind_idx[batch.kind_first[kind] + i];
                 ++seen[id];
                 const BatchChunk& c = batch.hv[id];
-                expect(ptrs[c.sec]->spans[c.block].kind == kind, "chunk listed under its kind", trial, id);
+                const int bk = ptrs[c.sec]->spans[c.block].kind;
+                const int want = bk == kRowsFree && ptrs[c.sec]->seg_win == 64 ? kRowsFree64 : bk;
+                expect(want == kind, "chunk listed under its kind", trial, id);
             }
         for (int v : seen) expect(v == 1, "every chunk listed once", trial, v);
     }

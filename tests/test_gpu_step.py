@@ -126,3 +126,59 @@ def test_step_shapes(cuda, key, precision):
     for bad in ((3, 16384, 0), (-1, 16384, 0), (1, 12288, 0), (1, 512, 0), (2, 131072, 0), (1, 16384, 2)):
         with pytest.raises(nat.EngineError):
             autotune.set_step_shape(sec, *bad)
+
+
+@pytest.mark.parametrize("key", [(12, 2, 11, 0, 0), (12, 2, 11, 5, 1)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("weights", ["merged", "split"])
+def test_segment_windows(cuda, key, precision, weights):
+    """64-offset segment windows (a lane's two rows in one segment): every launch variant gives the
+    same bits, y = H v to the form's tolerance, staged gathers refused with them, and a sector
+    re-planned back to 32-offset windows gives its first bits again."""
+    torch = cuda
+    from exactdiag_gb300 import _native as nat
+    from exactdiag_gb300 import autotune
+    from exactdiag_gb300.engine import DeviceSector
+
+    w = W if weights == "merged" else {"tl": 1.0, "tr": 0.7, "jl": 0.5, "jr": 0.3}
+    sec = DeviceSector(*key)
+    dt = sec.dtype(precision)
+    x = seeded_vector(sec.n, 29, not sec.is_real)
+    v = torch.as_tensor(x if not sec.is_real else x.real, device=sec.device).to(dt)
+    ref = sec.hv_mode(v, w, 0)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    scale = max(1.0, float(torch.max(torch.abs(ref)).item()))
+
+    def step():
+        y = torch.zeros_like(v)
+        scal = torch.zeros(8, dtype=torch.float64, device=sec.device)
+        sec.lanczos_hv(w, v, None, y, scal[0:4])
+        torch.cuda.synchronize()
+        return y, scal[:4].cpu().numpy()
+
+    first_y, first_s = step()
+    assert autotune.get_window(sec) == 32
+    autotune.set_window(sec, 64)
+    assert autotune.get_window(sec) == 64
+    y64, s64 = step()
+    assert float(torch.max(torch.abs(y64 - ref)).item()) <= tol * scale
+    assert abs(s64[1] - first_s[1]) <= 1e-9 * max(1.0, abs(first_s[1])) * (1 if precision == "fp64" else 1e3)
+    for minb, ctas in autotune.CANDIDATES:
+        for nr in (1, 2):
+            autotune.set_launch(sec, minb, ctas)
+            autotune.set_step_shape(sec, nr, autotune.DEFAULT_CHUNK_ROWS, 0)
+            y, s = step()
+            assert torch.equal(y, y64) and np.array_equal(s, s64), (minb, ctas, nr)
+    with pytest.raises(nat.EngineError):
+        autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS, 1)
+    for bad in (0, 16, 48, 128):
+        with pytest.raises(nat.EngineError):
+            autotune.set_window(sec, bad)
+    autotune.set_window(sec, 32)
+    autotune.set_launch(sec, 3, 0)
+    autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS, 1)
+    with pytest.raises(nat.EngineError):
+        autotune.set_window(sec, 64)
+    autotune.set_step_shape(sec, 0, autotune.DEFAULT_CHUNK_ROWS, 0)
+    y, s = step()
+    assert torch.equal(y, first_y) and np.array_equal(s, first_s)

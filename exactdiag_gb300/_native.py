@@ -53,6 +53,7 @@ SIGNATURES = {
     "ed_lanczos_hv": (_c.c_int, [_vp, _d4, _c.c_int, _vp, _vp, _vp, _vp, _vp]),
     "ed_lanczos_update": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp, _vp]),
     "ed_accumulate": (_c.c_int, [_vp, _c.c_int, _vp, _c.c_double, _c.c_double, _vp, _vp]),
+    "ed_accumulate_many": (_c.c_int, [_vp, _c.c_int, _c.c_int, _c.POINTER(_c.c_void_p), _c.POINTER(_c.c_double), _vp, _vp]),
     "ed_normalize": (_c.c_int, [_vp, _c.c_int, _vp, _vp, _vp]),
     "ed_continued_fraction": (_c.c_int, [_vp, _vp, _c.c_int, _vp, _c.c_int, _c.c_double, _c.c_double, _c.c_double,
                                          _vp, _vp]),

@@ -328,6 +328,20 @@ int ed_accumulate(const ed_sector* h, int dtype, const void* x_dev, double coef_
     return accumulate_launch(h->s, dtype, x_dev, coef_re, coef_im, acc_dev, (cudaStream_t)stream);
 }
 
+int ed_accumulate_many(const ed_sector* h, int dtype, int k, const void* const* x_devs, const double* coefs,
+                       void* acc_dev, void* stream) {
+    if (h && h->s.built && h->s.view.n == 0) return ED_OK;
+    if (!h || !acc_dev || k < 0 || (k > 0 && (!x_devs || !coefs)))
+        return set_error(ED_ERR_INVALID, "ed_accumulate_many: NULL argument or k < 0");
+    if (!h->s.built) return set_error(ED_ERR_NOT_BUILT, "ed_accumulate_many: basis not built");
+    for (int j = 0; j < k; ++j) {
+        if (!x_devs[j]) return set_error(ED_ERR_INVALID, "ed_accumulate_many: NULL vector");
+        if (!std::isfinite(coefs[2 * j]) || !std::isfinite(coefs[2 * j + 1]))
+            return set_error(ED_ERR_INVALID, "ed_accumulate_many: coef");
+    }
+    return accumulate_many_launch(h->s, dtype, k, x_devs, coefs, acc_dev, (cudaStream_t)stream);
+}
+
 int ed_normalize(const ed_sector* h, int dtype, void* x_dev, double* norm_dev, void* stream) {
     if (h && h->s.built && h->s.view.n == 0) return set_error(ED_ERR_INVALID, "ed_normalize: empty sector");
     if (!h || !x_dev || !norm_dev) return set_error(ED_ERR_INVALID, "ed_normalize: NULL argument");

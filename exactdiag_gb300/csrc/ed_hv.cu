@@ -114,6 +114,17 @@ int hv_launch(const Sector& s, const HvWeights& w, int dtype, const void* x, voi
     }
 }
 
+// acc_i += c x_i as explicit fused multiply-adds in a fixed order, so that one vector at a time
+// (accumulate_kernel) and several in one pass (accumulate_many_kernel) give the same bits.
+template <typename R, bool CPLX>
+__device__ __forceinline__ void acc_term(double& ar, double& ai, double cr, double ci, R xr, R xi) {
+    ar = __fma_rn(cr, (double)xr, ar);
+    if constexpr (CPLX) {
+        ar = __fma_rn(-ci, (double)xi, ar);
+        ai = __fma_rn(ci, (double)xr, __fma_rn(cr, (double)xi, ai));
+    }
+}
+
 template <typename R, bool CPLX>
 __global__ void accumulate_kernel(int64_t n, const void* __restrict__ x, double cr, double ci, void* __restrict__ acc) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -122,12 +133,44 @@ __global__ void accumulate_kernel(int64_t n, const void* __restrict__ x, double 
         if constexpr (CPLX) {
             double2* a = reinterpret_cast<double2*>(acc) + i;
             double2 t = *a;
-            t.x += cr * (double)xr - ci * (double)xi;
-            t.y += cr * (double)xi + ci * (double)xr;
+            acc_term<R, CPLX>(t.x, t.y, cr, ci, xr, xi);
             *a = t;
         } else {
-            reinterpret_cast<double*>(acc)[i] += cr * (double)xr;
+            double* a = reinterpret_cast<double*>(acc) + i;
+            double t = *a, unused = 0.0;
+            acc_term<R, CPLX>(t, unused, cr, ci, xr, xi);
+            *a = t;
         }
+    }
+}
+
+// Up to kAccumMany vectors and their coefficients, passed by value.
+struct AccumMany {
+    const void* x[kAccumMany];
+    double cr[kAccumMany], ci[kAccumMany];
+    int k;
+};
+
+// acc_i += sum_j c_j x_{j,i}, the terms added in order j = 0, 1, ... exactly as k calls of
+// accumulate_kernel would, reading and writing acc once.
+template <typename R, bool CPLX>
+__global__ void accumulate_many_kernel(int64_t n, const AccumMany m, void* __restrict__ acc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double ar, ai = 0.0;
+        if constexpr (CPLX) {
+            const double2 t = reinterpret_cast<const double2*>(acc)[i];
+            ar = t.x;
+            ai = t.y;
+        } else {
+            ar = reinterpret_cast<const double*>(acc)[i];
+        }
+        for (int j = 0; j < m.k; ++j) {
+            R xr, xi;
+            ld<R, CPLX>(m.x[j], i, xr, xi);
+            acc_term<R, CPLX>(ar, ai, m.cr[j], m.ci[j], xr, xi);
+        }
+        if constexpr (CPLX) reinterpret_cast<double2*>(acc)[i] = make_double2(ar, ai);
+        else reinterpret_cast<double*>(acc)[i] = ar;
     }
 }
 
@@ -142,6 +185,30 @@ int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, doub
     default: accumulate_kernel<float, true><<<g, 256, 0, st>>>(s.view.n, x, cr, ci, acc); break;
     }
     ED_CHECK_LAUNCH("accumulate_kernel");
+    return ED_OK;
+}
+
+int accumulate_many_launch(const Sector& s, int dtype, int k, const void* const* xs, const double* coefs, void* acc,
+                           cudaStream_t st) {
+    if (!dtype_ok(s, dtype)) return set_error(ED_ERR_INVALID, "ed_accumulate_many: dtype does not match the sector");
+    if (s.view.n == 0 || k == 0) return ED_OK;
+    const int g = grid_for(s.view.n, 256, s.num_sms, 16);
+    for (int j0 = 0; j0 < k; j0 += kAccumMany) {
+        AccumMany m{};
+        m.k = std::min(kAccumMany, k - j0);
+        for (int j = 0; j < m.k; ++j) {
+            m.x[j] = xs[j0 + j];
+            m.cr[j] = coefs[2 * (j0 + j)];
+            m.ci[j] = coefs[2 * (j0 + j) + 1];
+        }
+        switch (dtype) {
+        case ED_F64: accumulate_many_kernel<double, false><<<g, 256, 0, st>>>(s.view.n, m, acc); break;
+        case ED_C128: accumulate_many_kernel<double, true><<<g, 256, 0, st>>>(s.view.n, m, acc); break;
+        case ED_F32: accumulate_many_kernel<float, false><<<g, 256, 0, st>>>(s.view.n, m, acc); break;
+        default: accumulate_many_kernel<float, true><<<g, 256, 0, st>>>(s.view.n, m, acc); break;
+        }
+        ED_CHECK_LAUNCH("accumulate_many_kernel");
+    }
     return ED_OK;
 }
 

@@ -244,6 +244,9 @@ int lanczos_hv_launch(const Sector& s, const HvWeights& w, int dtype, const void
                       double* scal, double* partials, cudaStream_t st);
 int lanczos_update_launch(const Sector& s, int dtype, const void* v, void* vnext, const double* scal, cudaStream_t st);
 int accumulate_launch(const Sector& s, int dtype, const void* x, double cr, double ci, void* acc, cudaStream_t st);
+constexpr int kAccumMany = 32;  // vectors one accumulate_many_kernel launch takes (the rest in further launches)
+int accumulate_many_launch(const Sector& s, int dtype, int k, const void* const* xs, const double* coefs, void* acc,
+                           cudaStream_t st);
 int normalize_launch(const Sector& s, int dtype, void* x, double* norm, double* partials, cudaStream_t st);
 int single_setup(Sector& s);
 int build_descriptors(Sector& s);

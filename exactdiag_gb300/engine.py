@@ -174,6 +174,29 @@ class DeviceSector:
         nat.check("ed_accumulate",
                   self._lib.ed_accumulate(self._h, code, _ptr(x), c.real, c.imag, _ptr(acc), _stream_ptr()))
 
+    def accumulate_many(self, xs: list, coefs: list, acc: torch.Tensor) -> None:
+        """acc += sum_j coefs[j] * xs[j] in one pass over acc (ed_accumulate_many): the same bits as
+        accumulate() called for each j in order."""
+        if len(xs) != len(coefs):
+            raise ValueError("one coefficient per vector")
+        if not xs:
+            return
+        code = self._code(xs[0])
+        want = torch.float64 if self.is_real else torch.complex128
+        if acc.dtype != want or not acc.is_cuda or acc.numel() != self.n:
+            raise ValueError(f"acc must be a {want} CUDA tensor of length n")
+        for x in xs:
+            if x.dtype != xs[0].dtype or not x.is_cuda or not x.is_contiguous() or x.numel() != self.n:
+                raise ValueError("the vectors must be contiguous CUDA tensors of one dtype and length n")
+        k = len(xs)
+        ptrs = (ctypes.c_void_p * k)(*[x.data_ptr() for x in xs])
+        cf = (ctypes.c_double * (2 * k))()
+        for j, c in enumerate(coefs):
+            c = complex(c)
+            cf[2 * j], cf[2 * j + 1] = c.real, c.imag
+        nat.check("ed_accumulate_many",
+                  self._lib.ed_accumulate_many(self._h, code, k, ptrs, cf, _ptr(acc), _stream_ptr()))
+
     def project_out(self, basis: torch.Tensor, k: int, w: torch.Tensor, coef_out: torch.Tensor | None = None) -> None:
         """w <- w - sum_{j<k} <basis[j], w> basis[j] (ed_project_out); coef_out float64 (2k,) gets the dots."""
         code = self._code(w)

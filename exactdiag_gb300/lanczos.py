@@ -174,8 +174,8 @@ class CheckedLanczos:
         kept = min(self.keep, self.steps)
         if kept < 2 and kept < self.steps:
             kept = 0  # too few kept to continue from: regenerate from v0
-        for k in range(kept):
-            s.accumulate(self.V[k], complex(self.s[k]), acc)
+        # the kept vectors in one pass over acc (the same bits as one accumulate per vector)
+        s.accumulate_many(self.V[:kept], [complex(self.s[k]) for k in range(kept)], acc)
         if kept == self.steps:
             return acc
         if kept >= 2:

@@ -155,6 +155,13 @@ int ed_lanczos_update(const ed_sector* s, int dtype, const void* v_dev, void* v_
 int ed_accumulate(const ed_sector* s, int dtype, const void* x_dev, double coef_re, double coef_im, void* acc_dev,
                   void* stream);
 
+/* acc += sum_j (coefs[2j] + i coefs[2j+1]) * x_devs[j] for j < k in one pass over acc (x_devs and
+ * coefs are host arrays of k device pointers and 2k doubles): the same bits as k calls of
+ * ed_accumulate in that order, with acc read and written once per 32 vectors instead of once per
+ * vector.  ED_ERR_INVALID for k < 0, a NULL vector or a non-finite coefficient. */
+int ed_accumulate_many(const ed_sector* s, int dtype, int k, const void* const* x_devs, const double* coefs,
+                       void* acc_dev, void* stream);
+
 /* Scales x in place to unit norm (FP64 accumulation); norm written to norm_dev[0]. */
 int ed_normalize(const ed_sector* s, int dtype, void* x_dev, double* norm_dev, void* stream);
 

@@ -353,3 +353,31 @@ def test_mixed_ground_state_kept_and_regenerated_vectors_agree(torch, oracle, ke
         assert g["steps"] == runs[0]["steps"] and g["refine_steps"] == runs[0]["refine_steps"]
     assert runs[0]["E0"] == runs[1]["E0"] == runs[2]["E0"]
     assert runs[0]["kept_vectors"] == runs[0]["steps"] and runs[1]["kept_vectors"] == 7 and runs[2]["kept_vectors"] == 0
+
+
+@pytest.mark.parametrize("key", [(6, 2, 5, 0, 0), (6, 2, 5, 1, 0)])
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_accumulate_many_equals_one_at_a_time(torch, key, precision):
+    """ed_accumulate_many gives the bits of ed_accumulate called once per vector, across its
+    32-vector launches, and refuses a NULL vector and a non-finite coefficient."""
+    from exactdiag_gb300 import _native as nat
+
+    sec = _sector(key)
+    dt = sec.dtype(precision)
+    rng = np.random.default_rng(11)
+    xs = []
+    for _ in range(40):
+        x = rng.uniform(-1, 1, sec.n) + (0j if sec.is_real else 1j * rng.uniform(-1, 1, sec.n))
+        xs.append(torch.as_tensor(x.real if sec.is_real else x, device="cuda").to(dt))
+    coefs = [complex(c) if not sec.is_real else complex(c.real) for c in rng.normal(size=40) + 1j * rng.normal(size=40)]
+    acc_t = torch.float64 if sec.is_real else torch.complex128
+    start = torch.as_tensor(rng.uniform(-1, 1, sec.n), device="cuda").to(acc_t)
+    one = start.clone()
+    for x, c in zip(xs, coefs):
+        sec.accumulate(x, c, one)
+    many = start.clone()
+    sec.accumulate_many(xs, coefs, many)
+    torch.cuda.synchronize()
+    assert torch.equal(one, many)
+    with pytest.raises(nat.EngineError):
+        sec.accumulate_many(xs[:2], [1.0, float("nan")], many)

@@ -254,7 +254,8 @@ def form_rates(sec, dt, K: int, W: int) -> dict:
     out = {"dtype": str(dt).replace("torch.", ""), "steps_per_s": 1000.0 * K / t["total_ms"],
            "ms_per_step": t["total_ms"] / K, "hv_ms": hv, "hv_gbs": gbs, "frac": gbs / peak}
     if rec:
-        out["launch"] = {"min_ctas_per_sm": rec["min_ctas_per_sm"], "ctas_per_sm": rec["ctas_per_sm"]}
+        out["launch"] = {k: rec.get(k) for k in ("min_ctas_per_sm", "ctas_per_sm", "rows_per_lane", "staged",
+                                                 "window", "chunk_rows")}
     return out
 
 
